@@ -1,0 +1,136 @@
+/* stonewall.h -- C ABI of the GB300 (sm_103a) D3Q19 wall-wind solver.
+ *
+ * Drop-in for the Warp kernels of stonewall3d/lbm3d.py (Cat-yejun/jeju-stonewall-lbm).
+ * Each entry point below replaces one `wp.launch(k_*, dim=..., inputs=[...])`
+ * call of the reference; the citation beside it names the kernel and the call
+ * site.  As in the reference, the caller owns every device buffer (the driver
+ * allocates them, lbm3d.py:292-313) and the entry points only launch work on
+ * the given stream; they return an SW_* status instead of raising.
+ *
+ * Device layout (x fastest; the reference's arrays are z fastest):
+ *   f      [19][nz][ny][pitch] of the storage type (sw_dtype_size)
+ *   flag   [nz][ny][pitch]     uint8, 0 fluid / 1 stone / 2 ground (lbm3d.py:30)
+ *   tiles  [nz][ny][pitch/32]  uint8, derived from flag by sw_build_tiles
+ *   u      [4][nz][ny][pitch]  float: rho, ux, uy, uz (lbm3d.py:158-182)
+ *   acc    [4][nz][ny][pitch]  double time sums of u
+ *   force  [n_t][nz][2]        int64, fixed point with 2^-40 units (SW_FORCE_SCALE):
+ *                              x and z momentum-exchange force per height level
+ *                              and step, as force[t][z][0..1] in lbm3d.py:99-101
+ * pitch = nx rounded up to a multiple of 32 (sw_geom_make).  Cells with
+ * x >= nx are padding and are never read or written by the step.
+ *
+ * The D3Q19 tables that the reference passes as arrays (cx, cy, cz, w, opp,
+ * mirz; lbm3d.py:20-28, 297-300) are compiled in, in the reference's order.
+ * Nothing here allocates device memory or synchronises the device unless its
+ * comment says so.
+ */
+#ifndef STONEWALL_H
+#define STONEWALL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+enum {
+  SW_OK = 0,
+  SW_ERR_BAD_ARG = 1,     /* null pointer, bad extent, unknown dtype, inconsistent geometry */
+  SW_ERR_OOM = 2,         /* reserved for callers that allocate (the library never does) */
+  SW_ERR_NONFINITE = 3,   /* a non-finite density or velocity was found (sw_check_finite) */
+  SW_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+  SW_ERR_CUDA = 5,        /* a CUDA call failed; sw_last_cuda_error() has the code */
+  SW_ERR_UNSUPPORTED = 6  /* valid request this build does not implement */
+};
+
+/* storage type of the distributions */
+enum {
+  SW_F32 = 0,        /* float32, as the reference (lbm3d.py:293-294) */
+  SW_F64 = 1,        /* float64 storage and arithmetic (the precision oracle run) */
+  SW_F16_SHIFT = 2,  /* binary16 holding f_i - w_i, float32 collision */
+  SW_BF16_SHIFT = 3  /* bfloat16 holding f_i - w_i, float32 collision */
+};
+
+/* cell flags (lbm3d.py:30) */
+enum { SW_FLUID = 0, SW_WALL = 1, SW_GROUND = 2 };
+
+/* noise distributions of sw_init */
+enum { SW_NOISE_UNIFORM = 0, SW_NOISE_GAUSSIAN = 1 };
+
+#define SW_FORCE_SCALE 1099511627776.0 /* 2^40 fixed-point units per force unit */
+
+typedef void *sw_stream; /* a cudaStream_t; NULL is the legacy default stream */
+
+typedef struct sw_geom {
+  int32_t nx, ny, nz; /* cells along x (wind), y (span, periodic), z (height) */
+  int32_t pitch;      /* padded x extent of the device layout */
+} sw_geom;
+
+/* ---------------------------------------------------------------- library */
+const char *sw_version(void);
+const char *sw_status_string(int status);
+/* cudaError_t of the last CUDA failure reported as SW_ERR_CUDA by this thread. */
+int sw_last_cuda_error(void);
+
+/* ---------------------------------------------------------------- geometry and sizes
+ * Replaces the shape arithmetic of lbm3d.py:270, 283, 293-303. */
+int sw_geom_make(int32_t nx, int32_t ny, int32_t nz, sw_geom *out);
+int64_t sw_cells_padded(const sw_geom *g);   /* nz * ny * pitch */
+int64_t sw_lattice_elems(const sw_geom *g);  /* 19 * nz * ny * pitch */
+int64_t sw_tile_count(const sw_geom *g);     /* nz * ny * pitch / 32 */
+size_t sw_dtype_size(int dtype);             /* bytes per stored population, 0 if unknown */
+
+/* ---------------------------------------------------------------- layout conversion
+ * The reference's host<->device copies (wp.array(flag) lbm3d.py:295, f0.assign
+ * lbm3d.py:332, f0.numpy() lbm3d.py:345) use its z-fastest layout; these
+ * device-to-device transposes convert to and from it.  ref_dtype is SW_F32 or
+ * SW_F64 (the type of the reference-layout array). */
+int sw_pack_flag(const sw_geom *g, const uint8_t *flag_ref, uint8_t *flag, sw_stream s);
+int sw_pack_f(const sw_geom *g, int dtype, int ref_dtype, const void *f_ref, void *f, sw_stream s);
+int sw_unpack_f(const sw_geom *g, int dtype, int ref_dtype, const void *f, void *f_ref, sw_stream s);
+/* u / acc in the device layout -> [4][nx][ny][nz] float (u) or double (acc). */
+int sw_unpack_u(const sw_geom *g, const float *u, float *u_ref, sw_stream s);
+int sw_unpack_acc(const sw_geom *g, const double *acc, double *acc_ref, sw_stream s);
+
+/* Classify every 32-cell row segment (fluid-only fast path, stone contact,
+ * all solid).  Must be rerun whenever flag changes.  Has no reference
+ * counterpart: it replaces the per-cell neighbour flag tests of
+ * lbm3d.py:88-95 where they cannot fire. */
+int sw_build_tiles(const sw_geom *g, const uint8_t *flag, uint8_t *tiles, sw_stream s);
+
+/* ---------------------------------------------------------------- kernels */
+/* k_init, lbm3d.py:39-54 (launched at lbm3d.py:340): equilibrium at rho = 1
+ * with the inlet speed uin[z] perturbed per fluid cell; solids at rest.
+ * noise_kind SW_NOISE_UNIFORM follows the reference (u0*(1+noise*(2r-1)), ...),
+ * SW_NOISE_GAUSSIAN draws standard normals instead.  The random stream is a
+ * PCG hash of (seed, cell) in the form rand_init(seed, (x*7919+y)*7907+z). */
+int sw_init(const sw_geom *g, int dtype, void *f, const uint8_t *flag, const float *uin, float noise,
+            int32_t seed, int32_t noise_kind, sw_stream s);
+
+/* k_step, lbm3d.py:57-155 (launched at lbm3d.py:359-361): one fused timestep
+ * f_in -> f_out: pull streaming (periodic y, outlet copy, free-slip top),
+ * half-way bounce-back, momentum-exchange force into force[t][z][0..1] (added
+ * atomically: the row must hold zero, or the partial sum to add to), regularized
+ * BGK with the Smagorinsky time scale and the outlet sponge.  Non-fluid cells of
+ * f_out are not written, as in the reference.  force may be NULL (no force). */
+int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
+            const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge,
+            double nu_sponge, int64_t *force, int64_t t, sw_stream s);
+
+/* k_macro, lbm3d.py:158-182 (lbm3d.py:367, 387): u = (rho, ux, uy, uz); solids -> (1, 0, 0, 0). */
+int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s);
+/* k_accum, lbm3d.py:185-188 (lbm3d.py:369): acc += u, in double. */
+int sw_accum(const sw_geom *g, const float *u, double *acc, sw_stream s);
+/* k_macro followed by k_accum (lbm3d.py:367-369) in one pass; u may be NULL. */
+int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, double *acc,
+                   sw_stream s);
+
+/* force rows (fixed point) -> double, n values. */
+int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STONEWALL_H */

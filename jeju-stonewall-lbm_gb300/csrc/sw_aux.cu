@@ -1,0 +1,315 @@
+// sw_aux.cu -- k_init, k_macro / k_accum, tile classification and layout transposes.
+//
+// This translation unit is compiled with --fmad=false: these kernels run once
+// (or every few steps) and evaluate every expression in source order, so their
+// float32 results equal the reference's operation sequence exactly (k_init for
+// the same random stream, k_macro for the same f).
+#include "sw_aux.cuh"
+
+namespace sw {
+
+// ---------------------------------------------------------------- random stream
+// PCG hash (Jarzynski & Olano, JCGT 2020), used as rand_init(seed, offset) =
+// pcg(seed + pcg(offset)) and randf(state) = (pcg(state) >> 8) / 2^24 -- the
+// form of the wp.rand_init / wp.randf calls in lbm3d.py:48-52.
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t s) {
+  uint32_t b = s * 747796405u + 2891336453u;
+  uint32_t c = ((b >> ((b >> 28u) + 4u)) ^ b) * 277803737u;
+  return (c >> 22u) ^ c;
+}
+__device__ __forceinline__ float randf(uint32_t &st) {
+  st = pcg_hash(st);
+  return (float)(st >> 8) * (1.0f / 16777216.0f);
+}
+__device__ __forceinline__ float gauss_pair(uint32_t &st, float *second) {
+  double u1 = 1.0 - (double)randf(st);
+  double u2 = (double)randf(st);
+  double r = sqrt(-2.0 * log(u1));
+  double a = 6.283185307179586 * u2;
+  if (second) *second = (float)(r * sin(a));
+  return (float)(r * cos(a));
+}
+
+// k_init, lbm3d.py:39-54.  One thread per cell of the padded grid.
+template <int DT>
+__global__ void k_init(Geom g, typename Store<DT>::T *f, const uint8_t *flag, const float *uin, float noise,
+                       int seed, int noise_kind) {
+  using S = Store<DT>;
+  using R = typename S::R;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.plane) return;
+  const int x = (int)(c % g.pitch);
+  const long long row = c / g.pitch;
+  const int y = (int)(row % g.ny), z = (int)(row / g.ny);
+  if (x >= g.nx) return;
+  R ux = R(0.0), uy = R(0.0), uz = R(0.0);
+  if (flag[c] == 0) {
+    const uint32_t off = ((uint32_t)x * 7919u + (uint32_t)y) * 7907u + (uint32_t)z;
+    uint32_t st = pcg_hash((uint32_t)seed + pcg_hash(off));
+    const R u0 = (R)uin[z];
+    const R nz_ = (R)noise;
+    if (noise_kind == SW_NOISE_UNIFORM) {
+      ux = u0 * (R(1.0) + nz_ * (R(2.0) * (R)randf(st) - R(1.0)));
+      uy = u0 * nz_ * (R(2.0) * (R)randf(st) - R(1.0));
+      uz = u0 * nz_ * (R(2.0) * (R)randf(st) - R(1.0));
+    } else {
+      float g2 = 0.0f;
+      const float g1 = gauss_pair(st, &g2);
+      const float g3 = gauss_pair(st, nullptr);
+      ux = u0 * (R(1.0) + nz_ * (R)g1);
+      uy = u0 * nz_ * (R)g2;
+      uz = u0 * nz_ * (R)g3;
+    }
+  }
+  const size_t plane = (size_t)g.plane;
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const R v = feq_i<R>(W<R>(i), R(CX(i)), R(CY(i)), R(CZ(i)), R(1.0), ux, uy, uz);
+    f[(size_t)i * plane + c] = S::template enc<i>(v);
+  });
+}
+
+// k_macro (lbm3d.py:158-182) with an optional fused k_accum (lbm3d.py:185-188) in double.
+template <int DT>
+__global__ void k_macro(Geom g, const typename Store<DT>::T *f, const uint8_t *flag, float *u, double *acc) {
+  using S = Store<DT>;
+  using R = typename S::R;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.plane) return;
+  if ((int)(c % g.pitch) >= g.nx) return;
+  const size_t P = (size_t)g.plane;
+  R out[4];
+  if (flag[c] != 0) {
+    out[0] = R(1.0); out[1] = R(0.0); out[2] = R(0.0); out[3] = R(0.0);
+  } else {
+    R rho = R(0.0), mx = R(0.0), my = R(0.0), mz = R(0.0);
+    static_for<0, Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      const R v = S::template dec<i>(f[(size_t)i * P + c]);
+      rho += v;
+      mx += v * R(CX(i));
+      my += v * R(CY(i));
+      mz += v * R(CZ(i));
+    });
+    out[0] = rho; out[1] = mx / rho; out[2] = my / rho; out[3] = mz / rho;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (u) u[k * P + c] = (float)out[k];
+    if (acc) acc[k * P + c] += (double)out[k];
+  }
+}
+
+__global__ void k_accum(Geom g, const float *u, double *acc) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= 4 * g.plane) return;
+  if ((int)(c % g.pitch) >= g.nx) return;
+  acc[c] += (double)u[c];
+}
+
+// Segment classification for the step kernel (see TILE_* in sw_common.cuh).
+// Mirrors the pull-source mapping of the step (lbm3d.py:77-88).
+__global__ void k_build_tiles(Geom g, const uint8_t *flag, uint8_t *tiles) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nseg = (long long)g.nseg_x * g.ny * g.nz;
+  const long long seg = c >> 5;
+  if (seg >= nseg) return;  // whole warps only (plane is a multiple of 32)
+  const int lane = threadIdx.x & 31;
+  const int x = (int)(c % g.pitch);
+  const long long row = c / g.pitch;
+  const int y = (int)(row % g.ny), z = (int)(row / g.ny);
+  const bool live = x < g.nx;
+  bool fluid = false, nonfluid_src = false, wall_src = false;
+  if (live) {
+    fluid = flag[c] == 0;
+    if (fluid && x > 0) {  // inlet cells do not pull
+      const int ym = (y == 0) ? g.ny - 1 : y - 1, yp = (y == g.ny - 1) ? 0 : y + 1;
+      const int zp = (z == g.nz - 1) ? z : z + 1;
+      const int xp = (x + 1 >= g.nx) ? x : x + 1;
+      for (int i = 1; i < Q; ++i) {
+        const int ex = CX(i), ey = CY(i), ez = CZ(i);
+        if (ez == 1 && z == 0) { nonfluid_src = true; continue; }
+        const int xs = ex == 1 ? x - 1 : (ex == -1 ? xp : x);
+        const int ys = ey == 1 ? ym : (ey == -1 ? yp : y);
+        const int zs = ez == 1 ? z - 1 : (ez == -1 ? zp : z);
+        const uint8_t fs = flag[((long long)zs * g.ny + ys) * g.pitch + xs];
+        if (fs != 0) nonfluid_src = true;
+        if (fs == SW_WALL) wall_src = true;
+      }
+    }
+  }
+  const unsigned any_fluid = __ballot_sync(0xffffffffu, live && fluid);
+  const unsigned any_check = __ballot_sync(0xffffffffu, live && (!fluid || nonfluid_src));
+  const unsigned any_wall = __ballot_sync(0xffffffffu, live && fluid && wall_src);
+  if (lane == 0)
+    tiles[seg] = (uint8_t)((any_fluid ? 0 : TILE_ALL_SOLID) | (any_check ? TILE_CHECK : 0) |
+                           (any_wall ? TILE_FORCE : 0));
+}
+
+// ---------------------------------------------------------------- x <-> z transposes
+// Reference layout a[k][x][y][z] (z fastest) <-> device layout b[k][z][y][pitch].
+// One block moves a 32 x 32 tile of the (x, z) plane of one (k, y).
+template <typename A, typename B, typename Conv>
+__global__ void k_ref_to_dev(Geom g, int nk, const A *a, B *b, Conv conv) {
+  __shared__ A t[32][33];
+  const int ky = blockIdx.x;             // k * ny + y
+  const int k = ky / g.ny, y = ky % g.ny;
+  const int x0 = blockIdx.y * 32, z0 = blockIdx.z * 32;
+  const size_t aplane = (size_t)g.nx * g.ny * g.nz;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {   // r: x offset, threadIdx.x: z offset
+    const int x = x0 + r, z = z0 + threadIdx.x;
+    if (x < g.nx && z < g.nz) t[r][threadIdx.x] = a[k * aplane + ((size_t)x * g.ny + y) * g.nz + z];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {   // r: z offset, threadIdx.x: x offset
+    const int z = z0 + r, x = x0 + threadIdx.x;
+    if (x < g.pitch && z < g.nz) {
+      const size_t o = (size_t)k * g.plane + ((size_t)z * g.ny + y) * g.pitch + x;
+      if (x < g.nx) b[o] = conv(k, t[threadIdx.x][r]);
+      else b[o] = conv.pad(k);
+    }
+  }
+  (void)nk;
+}
+
+template <typename B, typename A, typename Conv>
+__global__ void k_dev_to_ref(Geom g, int nk, const B *b, A *a, Conv conv) {
+  __shared__ A t[32][33];
+  const int ky = blockIdx.x;
+  const int k = ky / g.ny, y = ky % g.ny;
+  const int x0 = blockIdx.y * 32, z0 = blockIdx.z * 32;
+  const size_t aplane = (size_t)g.nx * g.ny * g.nz;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {   // r: z offset, threadIdx.x: x offset
+    const int z = z0 + r, x = x0 + threadIdx.x;
+    if (x < g.nx && z < g.nz) t[r][threadIdx.x] = conv(k, b[(size_t)k * g.plane + ((size_t)z * g.ny + y) * g.pitch + x]);
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {   // r: x offset, threadIdx.x: z offset
+    const int x = x0 + r, z = z0 + threadIdx.x;
+    if (x < g.nx && z < g.nz) a[k * aplane + ((size_t)x * g.ny + y) * g.nz + z] = t[threadIdx.x][r];
+  }
+  (void)nk;
+}
+
+// Converters between a reference-layout value and the stored value of population k.
+template <int DT, typename A> struct EncF {
+  __device__ typename Store<DT>::T operator()(int k, A v) const { return enc_dyn(k, (typename Store<DT>::R)v); }
+  __device__ typename Store<DT>::T pad(int k) const { return enc_dyn(k, W<typename Store<DT>::R>(k)); }
+  static __device__ typename Store<DT>::T enc_dyn(int k, typename Store<DT>::R v) {
+    typename Store<DT>::T out{};
+    static_for<0, Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      if (k == i) out = Store<DT>::template enc<i>(v);
+    });
+    return out;
+  }
+};
+template <int DT, typename A> struct DecF {
+  __device__ A operator()(int k, typename Store<DT>::T v) const {
+    A out{};
+    static_for<0, Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      if (k == i) out = (A)Store<DT>::template dec<i>(v);
+    });
+    return out;
+  }
+};
+template <typename A> struct Ident {
+  __device__ A operator()(int, A v) const { return v; }
+  __device__ A pad(int) const { return A(0); }
+};
+
+inline dim3 tgrid(const Geom &g, int nk, int xext) {
+  return dim3((unsigned)(nk * g.ny), (unsigned)((xext + 31) / 32), (unsigned)((g.nz + 31) / 32));
+}
+
+template <int DT>
+cudaError_t pack_f_t(const Geom &g, int ref_dtype, const void *ref, void *f, cudaStream_t s) {
+  using T = typename Store<DT>::T;
+  if (ref_dtype == SW_F32)
+    k_ref_to_dev<<<tgrid(g, Q, g.pitch), dim3(32, 8), 0, s>>>(g, Q, (const float *)ref, (T *)f, EncF<DT, float>{});
+  else
+    k_ref_to_dev<<<tgrid(g, Q, g.pitch), dim3(32, 8), 0, s>>>(g, Q, (const double *)ref, (T *)f, EncF<DT, double>{});
+  return cudaGetLastError();
+}
+template <int DT>
+cudaError_t unpack_f_t(const Geom &g, int ref_dtype, const void *f, void *ref, cudaStream_t s) {
+  using T = typename Store<DT>::T;
+  if (ref_dtype == SW_F32)
+    k_dev_to_ref<<<tgrid(g, Q, g.nx), dim3(32, 8), 0, s>>>(g, Q, (const T *)f, (float *)ref, DecF<DT, float>{});
+  else
+    k_dev_to_ref<<<tgrid(g, Q, g.nx), dim3(32, 8), 0, s>>>(g, Q, (const T *)f, (double *)ref, DecF<DT, double>{});
+  return cudaGetLastError();
+}
+
+template <int DT>
+cudaError_t init_t(const Geom &g, void *f, const uint8_t *flag, const float *uin, float noise, int seed, int kind,
+                   cudaStream_t s) {
+  const long long blocks = (g.plane + 255) / 256;
+  k_init<DT><<<(unsigned)blocks, 256, 0, s>>>(g, (typename Store<DT>::T *)f, flag, uin, noise, seed, kind);
+  return cudaGetLastError();
+}
+template <int DT>
+cudaError_t macro_t(const Geom &g, const void *f, const uint8_t *flag, float *u, double *acc, cudaStream_t s) {
+  const long long blocks = (g.plane + 255) / 256;
+  k_macro<DT><<<(unsigned)blocks, 256, 0, s>>>(g, (const typename Store<DT>::T *)f, flag, u, acc);
+  return cudaGetLastError();
+}
+
+#define SW_DISPATCH(dtype, CALL)                         \
+  switch (dtype) {                                       \
+    case SW_F32: { constexpr int DT = SW_F32; return CALL; } \
+    case SW_F64: { constexpr int DT = SW_F64; return CALL; } \
+    case SW_F16_SHIFT: { constexpr int DT = SW_F16_SHIFT; return CALL; } \
+    case SW_BF16_SHIFT: { constexpr int DT = SW_BF16_SHIFT; return CALL; } \
+    default: return cudaErrorInvalidValue;               \
+  }
+
+cudaError_t aux_init(const Geom &g, int dtype, void *f, const uint8_t *flag, const float *uin, float noise, int seed,
+                     int kind, cudaStream_t s) {
+  SW_DISPATCH(dtype, init_t<DT>(g, f, flag, uin, noise, seed, kind, s));
+}
+cudaError_t aux_macro(const Geom &g, int dtype, const void *f, const uint8_t *flag, float *u, double *acc,
+                      cudaStream_t s) {
+  SW_DISPATCH(dtype, macro_t<DT>(g, f, flag, u, acc, s));
+}
+cudaError_t aux_accum(const Geom &g, const float *u, double *acc, cudaStream_t s) {
+  const long long blocks = (4 * g.plane + 255) / 256;
+  k_accum<<<(unsigned)blocks, 256, 0, s>>>(g, u, acc);
+  return cudaGetLastError();
+}
+cudaError_t aux_pack_f(const Geom &g, int dtype, int ref_dtype, const void *ref, void *f, cudaStream_t s) {
+  SW_DISPATCH(dtype, pack_f_t<DT>(g, ref_dtype, ref, f, s));
+}
+cudaError_t aux_unpack_f(const Geom &g, int dtype, int ref_dtype, const void *f, void *ref, cudaStream_t s) {
+  SW_DISPATCH(dtype, unpack_f_t<DT>(g, ref_dtype, f, ref, s));
+}
+cudaError_t aux_pack_flag(const Geom &g, const uint8_t *ref, uint8_t *flag, cudaStream_t s) {
+  k_ref_to_dev<<<tgrid(g, 1, g.pitch), dim3(32, 8), 0, s>>>(g, 1, ref, flag, Ident<uint8_t>{});
+  return cudaGetLastError();
+}
+cudaError_t aux_unpack_u(const Geom &g, const float *u, float *ref, cudaStream_t s) {
+  k_dev_to_ref<<<tgrid(g, 4, g.nx), dim3(32, 8), 0, s>>>(g, 4, u, ref, Ident<float>{});
+  return cudaGetLastError();
+}
+cudaError_t aux_unpack_acc(const Geom &g, const double *acc, double *ref, cudaStream_t s) {
+  k_dev_to_ref<<<tgrid(g, 4, g.nx), dim3(32, 8), 0, s>>>(g, 4, acc, ref, Ident<double>{});
+  return cudaGetLastError();
+}
+cudaError_t aux_build_tiles(const Geom &g, const uint8_t *flag, uint8_t *tiles, cudaStream_t s) {
+  const long long blocks = (g.plane + 255) / 256;
+  k_build_tiles<<<(unsigned)blocks, 256, 0, s>>>(g, flag, tiles);
+  return cudaGetLastError();
+}
+
+__global__ void k_force_to_f64(const long long *fx, double *out, long long n) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = (double)fx[k] * (1.0 / FORCE_SCALE);
+}
+cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_force_to_f64<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fx, out, n);
+  return cudaGetLastError();
+}
+
+}  // namespace sw

@@ -1,0 +1,28 @@
+// sw_aux.cuh -- host-side launchers of the kernels in sw_aux.cu and sw_step_*.cu.
+#pragma once
+#include "sw_common.cuh"
+
+namespace sw {
+
+struct StepParams;
+
+cudaError_t aux_init(const Geom &g, int dtype, void *f, const uint8_t *flag, const float *uin, float noise, int seed,
+                     int kind, cudaStream_t s);
+cudaError_t aux_macro(const Geom &g, int dtype, const void *f, const uint8_t *flag, float *u, double *acc,
+                      cudaStream_t s);
+cudaError_t aux_accum(const Geom &g, const float *u, double *acc, cudaStream_t s);
+cudaError_t aux_pack_f(const Geom &g, int dtype, int ref_dtype, const void *ref, void *f, cudaStream_t s);
+cudaError_t aux_unpack_f(const Geom &g, int dtype, int ref_dtype, const void *f, void *ref, cudaStream_t s);
+cudaError_t aux_pack_flag(const Geom &g, const uint8_t *ref, uint8_t *flag, cudaStream_t s);
+cudaError_t aux_unpack_u(const Geom &g, const float *u, float *ref, cudaStream_t s);
+cudaError_t aux_unpack_acc(const Geom &g, const double *acc, double *ref, cudaStream_t s);
+cudaError_t aux_build_tiles(const Geom &g, const uint8_t *flag, uint8_t *tiles, cudaStream_t s);
+cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cudaStream_t s);
+
+// one launcher per storage type, each in its own translation unit (sw_step_<dtype>.cu)
+cudaError_t step_f32(const StepParams &p, cudaStream_t s);
+cudaError_t step_f64(const StepParams &p, cudaStream_t s);
+cudaError_t step_f16s(const StepParams &p, cudaStream_t s);
+cudaError_t step_bf16s(const StepParams &p, cudaStream_t s);
+
+}  // namespace sw

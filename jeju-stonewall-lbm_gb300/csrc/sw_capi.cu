@@ -1,0 +1,173 @@
+// sw_capi.cu -- the extern "C" entry points declared in include/stonewall.h.
+//
+// Every entry point validates its arguments, launches on the caller's stream
+// and returns an SW_* status; nothing here allocates or synchronises.
+#include <cstdio>
+
+#include "sw_aux.cuh"
+#include "sw_step.cuh"
+
+namespace {
+
+thread_local int g_last_cuda = 0;
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return SW_OK;
+  g_last_cuda = (int)e;
+  return SW_ERR_CUDA;
+}
+
+bool geom_ok(const sw_geom *g) {
+  if (!g || g->nx <= 0 || g->ny <= 0 || g->nz <= 0) return false;
+  if (g->pitch != sw::round_up(g->nx, sw::SEG)) return false;
+  const long long cells = (long long)g->nz * g->ny * g->pitch;
+  return cells < (1ll << 31);
+}
+
+sw::Geom to_geom(const sw_geom *g) {
+  sw::Geom o;
+  o.nx = g->nx;
+  o.ny = g->ny;
+  o.nz = g->nz;
+  o.pitch = g->pitch;
+  o.nseg_x = g->pitch / sw::SEG;
+  o.plane = (long long)g->nz * g->ny * g->pitch;
+  return o;
+}
+
+bool dtype_ok(int dt) { return dt == SW_F32 || dt == SW_F64 || dt == SW_F16_SHIFT || dt == SW_BF16_SHIFT; }
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+cudaStream_t st(sw_stream s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace
+
+extern "C" {
+
+const char *sw_version(void) { return "stonewall-gb300 0.1 (sm_103a)"; }
+
+const char *sw_status_string(int status) {
+  switch (status) {
+    case SW_OK: return "ok";
+    case SW_ERR_BAD_ARG: return "bad argument";
+    case SW_ERR_OOM: return "out of device memory";
+    case SW_ERR_NONFINITE: return "non-finite state";
+    case SW_ERR_TIMEOUT: return "device wait timed out";
+    case SW_ERR_CUDA: return "CUDA error";
+    case SW_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int sw_last_cuda_error(void) { return g_last_cuda; }
+
+int sw_geom_make(int32_t nx, int32_t ny, int32_t nz, sw_geom *out) {
+  if (!out || nx <= 0 || ny <= 0 || nz <= 0) return SW_ERR_BAD_ARG;
+  sw_geom g{nx, ny, nz, sw::round_up(nx, sw::SEG)};
+  if (!geom_ok(&g)) return SW_ERR_BAD_ARG;
+  *out = g;
+  return SW_OK;
+}
+
+int64_t sw_cells_padded(const sw_geom *g) { return geom_ok(g) ? (int64_t)g->nz * g->ny * g->pitch : -1; }
+int64_t sw_lattice_elems(const sw_geom *g) { return geom_ok(g) ? (int64_t)sw::Q * g->nz * g->ny * g->pitch : -1; }
+int64_t sw_tile_count(const sw_geom *g) { return geom_ok(g) ? (int64_t)g->nz * g->ny * (g->pitch / sw::SEG) : -1; }
+
+size_t sw_dtype_size(int dtype) {
+  switch (dtype) {
+    case SW_F32: return 4;
+    case SW_F64: return 8;
+    case SW_F16_SHIFT: return 2;
+    case SW_BF16_SHIFT: return 2;
+    default: return 0;
+  }
+}
+
+int sw_pack_flag(const sw_geom *g, const uint8_t *flag_ref, uint8_t *flag, sw_stream s) {
+  if (!geom_ok(g) || !flag_ref || !flag) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_pack_flag(to_geom(g), flag_ref, flag, st(s)));
+}
+
+int sw_pack_f(const sw_geom *g, int dtype, int ref_dtype, const void *f_ref, void *f, sw_stream s) {
+  if (!geom_ok(g) || !dtype_ok(dtype) || (ref_dtype != SW_F32 && ref_dtype != SW_F64) || !f_ref || !f)
+    return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_pack_f(to_geom(g), dtype, ref_dtype, f_ref, f, st(s)));
+}
+
+int sw_unpack_f(const sw_geom *g, int dtype, int ref_dtype, const void *f, void *f_ref, sw_stream s) {
+  if (!geom_ok(g) || !dtype_ok(dtype) || (ref_dtype != SW_F32 && ref_dtype != SW_F64) || !f_ref || !f)
+    return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_unpack_f(to_geom(g), dtype, ref_dtype, f, f_ref, st(s)));
+}
+
+int sw_unpack_u(const sw_geom *g, const float *u, float *u_ref, sw_stream s) {
+  if (!geom_ok(g) || !u || !u_ref) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_unpack_u(to_geom(g), u, u_ref, st(s)));
+}
+
+int sw_unpack_acc(const sw_geom *g, const double *acc, double *acc_ref, sw_stream s) {
+  if (!geom_ok(g) || !acc || !acc_ref) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_unpack_acc(to_geom(g), acc, acc_ref, st(s)));
+}
+
+int sw_build_tiles(const sw_geom *g, const uint8_t *flag, uint8_t *tiles, sw_stream s) {
+  if (!geom_ok(g) || !flag || !tiles) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_build_tiles(to_geom(g), flag, tiles, st(s)));
+}
+
+int sw_init(const sw_geom *g, int dtype, void *f, const uint8_t *flag, const float *uin, float noise, int32_t seed,
+            int32_t noise_kind, sw_stream s) {
+  if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !uin || !aligned16(f)) return SW_ERR_BAD_ARG;
+  if (noise_kind != SW_NOISE_UNIFORM && noise_kind != SW_NOISE_GAUSSIAN) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_init(to_geom(g), dtype, f, flag, uin, noise, seed, noise_kind, st(s)));
+}
+
+int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
+            const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force, int64_t t,
+            sw_stream s) {
+  if (!geom_ok(g) || !dtype_ok(dtype) || !f_in || !f_out || !flag || !tiles || !uin) return SW_ERR_BAD_ARG;
+  if (f_in == f_out || !aligned16(f_in) || !aligned16(f_out) || t < 0) return SW_ERR_BAD_ARG;
+  sw::StepParams p;
+  p.fin = f_in;
+  p.fout = f_out;
+  p.flag = flag;
+  p.tiles = tiles;
+  p.uin = uin;
+  p.g = to_geom(g);
+  p.nu0 = nu0;
+  p.cs = cs;
+  p.nu_sponge = nu_sponge;
+  p.x_sponge = x_sponge;
+  p.force = force ? reinterpret_cast<long long *>(force) + (size_t)t * 2 * g->nz : nullptr;
+  cudaError_t e;
+  switch (dtype) {
+    case SW_F32: e = sw::step_f32(p, st(s)); break;
+    case SW_F64: e = sw::step_f64(p, st(s)); break;
+    case SW_F16_SHIFT: e = sw::step_f16s(p, st(s)); break;
+    default: e = sw::step_bf16s(p, st(s)); break;
+  }
+  return cuda_status(e);
+}
+
+int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s) {
+  if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !u) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_macro(to_geom(g), dtype, f, flag, u, nullptr, st(s)));
+}
+
+int sw_accum(const sw_geom *g, const float *u, double *acc, sw_stream s) {
+  if (!geom_ok(g) || !u || !acc) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_accum(to_geom(g), u, acc, st(s)));
+}
+
+int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, double *acc,
+                   sw_stream s) {
+  if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !acc) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_macro(to_geom(g), dtype, f, flag, u, acc, st(s)));
+}
+
+int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s) {
+  if (n < 0 || (n > 0 && (!force || !out))) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_force_to_f64(reinterpret_cast<const long long *>(force), out, n, st(s)));
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+"""Parity of the sm_103a step with the reference's kernels and the CPU oracle.
+
+Tolerances: the reference's float32 fields within 1e-5 relative (the parity bar
+for the plain FP32 form), wall forces within 1e-5 of the largest level force.
+The float64 storage kernel is held to 1e-12 against the float64 oracle.
+Kernels compiled without FMA contraction (init, macro) must be bit-exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from gpu_helpers import assert_fields_close, assert_force_close, gpu_run, inlet, make_mask
+
+pytestmark = pytest.mark.gpu
+
+RTOL_F32 = 1e-5
+RTOL_F64 = 1e-12
+
+
+def _params(d):
+    nu0, cs, x_sponge, nu_sponge, noise, seed, n = d["params"]
+    return float(np.float32(nu0)), float(np.float32(cs)), int(x_sponge), float(np.float32(nu_sponge)), \
+        float(np.float32(noise)), int(seed), int(n)
+
+
+@pytest.mark.parametrize("case", ["step_box", "step_rand"])
+def test_step_matches_reference_kernels(case, cuda):
+    d = golden(case)
+    nu0, cs, xs, nus, noise, seed, n = _params(d)
+    f, other, force = gpu_run(d["flag"], d["uin"], d["f_init"], nu0, cs, xs, nus, n)
+    assert_fields_close(f, d[f"f_step{n}"], d["flag"], RTOL_F32)
+    assert_fields_close(other, d[f"f_other{n}"], d["flag"], RTOL_F32)
+    assert_force_close(force, d["force"], RTOL_F32)
+
+
+@pytest.mark.parametrize("case", ["step_box", "step_rand"])
+def test_init_bit_exact(case, cuda):
+    from stonewall.fields import Flags, Grid, Lattice
+    from stonewall.kernels import DeviceVector, k_init
+    d = golden(case)
+    nu0, cs, xs, nus, noise, seed, n = _params(d)
+    nx, ny, nz = d["flag"].shape
+    grid = Grid(nx, ny, nz)
+    f = Lattice(grid, "f32")
+    k_init(f, Flags(grid, d["flag"]), DeviceVector(d["uin"]), noise, seed)
+    np.testing.assert_array_equal(f.numpy(), d["f_init"])
+
+
+def test_macro_and_accum_bit_exact(cuda):
+    from stonewall.fields import Accum, Flags, Grid, Lattice, Macro
+    from stonewall.kernels import k_accum, k_macro, k_macro_accum
+    d = golden("step_box")
+    n = int(d["params"][-1])
+    nx, ny, nz = d["flag"].shape
+    grid = Grid(nx, ny, nz)
+    flags = Flags(grid, d["flag"])
+    f = Lattice(grid, "f32").assign(d[f"f_step{n}"])
+    u = Macro(grid)
+    k_macro(f, flags, u)
+    np.testing.assert_array_equal(u.numpy(), d["macro"])
+    acc = Accum(grid)
+    k_accum(u, acc)
+    k_accum(u, acc)
+    np.testing.assert_array_equal(acc.numpy().astype(np.float32), d["accum2"])
+    acc2 = Accum(grid)
+    k_macro_accum(f, flags, acc2)
+    k_macro_accum(f, flags, acc2)
+    np.testing.assert_array_equal(acc2.numpy(), acc.numpy())
+
+
+def test_launch_mirror_matches_direct(cuda):
+    """launch(k_step, dim, [reference input list]) runs the same kernel as k_step()."""
+    from stonewall import kernels as K
+    from stonewall.fields import Flags, ForceSeries, Grid, Lattice
+    d = golden("step_rand")
+    nu0, cs, xs, nus, noise, seed, n = _params(d)
+    nx, ny, nz = d["flag"].shape
+    grid = Grid(nx, ny, nz)
+    flags = Flags(grid, d["flag"])
+    uv = K.DeviceVector(d["uin"])
+    cx, cy, cz, w, opp, mirz = K.tables_host()
+    f0, f1 = Lattice(grid), Lattice(grid).zero_()
+    K.launch(K.k_init, (nx, ny, nz), [f0, flags, uv, cx, cy, cz, w, noise, seed])
+    force = ForceSeries(n, nz)
+    for t in range(n):
+        K.launch(K.k_step, (nx, ny, nz), [f0, f1, flags, uv, cx, cy, cz, w, opp, mirz, nx, ny, nz, nu0, cs, xs,
+                                          nus, force, t])
+        f0, f1 = f1, f0
+    ref, _, ref_force = gpu_run(d["flag"], d["uin"], d["f_init"], nu0, cs, xs, nus, n)
+    np.testing.assert_array_equal(f0.numpy(), ref)
+    np.testing.assert_array_equal(force.numpy(), ref_force)
+    bad = cx.copy()
+    bad[1], bad[2] = bad[2], bad[1]
+    with pytest.raises(ValueError):
+        K.launch(K.k_step, (nx, ny, nz), [f0, f1, flags, uv, bad, cy, cz, w, opp, mirz, nx, ny, nz, nu0, cs, xs,
+                                          nus, force, 0])
+
+
+@pytest.mark.parametrize("shape,seed", [((64, 32, 33), 1), ((45, 7, 10), 2), ((96, 16, 17), 3)])
+def test_step_matches_oracle_f32(shape, seed, cuda, oracle_mod):
+    """Random stones on grids with padding (nx not a multiple of 32), odd ny, all boundaries."""
+    nx, ny, nz = shape
+    flag = make_mask(nx, ny, nz, seed)
+    uin = inlet(nz, max(2, nz // 4))
+    f0 = oracle_mod.init(flag, uin, noise=0.05, seed=seed)
+    args = (np.float32(2e-3), np.float32(0.1), nx - nx // 5, np.float32(0.05))
+    n = 10
+    want, want_force = oracle_mod.run(f0, flag, uin, *args[:3], n, args[3])
+    got, _, got_force = gpu_run(flag, uin, f0, *(float(a) for a in args[:2]), args[2], float(args[3]), n)
+    assert_fields_close(got, want, flag, RTOL_F32)
+    assert_force_close(got_force, want_force, RTOL_F32)
+
+
+def test_step_f64_matches_oracle_f64(cuda, oracle_mod):
+    nx, ny, nz = 40, 12, 15
+    flag = make_mask(nx, ny, nz, 5)
+    uin = inlet(nz, 4)
+    f0 = oracle_mod.init(flag, uin.astype(np.float64), noise=0.05, seed=5, dtype=np.float64)
+    n = 8
+    want, want_force = oracle_mod.run(f0, flag, uin.astype(np.float64), 2e-3, 0.1, 30, n, 0.05)
+    got, _, got_force = gpu_run(flag, uin, f0, 2e-3, 0.1, 30, 0.05, n, dtype="f64", ref_dtype=np.float64)
+    assert_fields_close(got, want, flag, RTOL_F64)
+    assert_force_close(got_force, want_force, 1e-10)
+
+
+def test_force_deterministic(cuda):
+    """Wall forces are bit-identical run to run (fixed-point accumulation)."""
+    d = golden("step_box")
+    nu0, cs, xs, nus, noise, seed, n = _params(d)
+    a = gpu_run(d["flag"], d["uin"], d["f_init"], nu0, cs, xs, nus, n)[2]
+    b = gpu_run(d["flag"], d["uin"], d["f_init"], nu0, cs, xs, nus, n)[2]
+    np.testing.assert_array_equal(a, b)

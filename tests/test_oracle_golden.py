@@ -1,0 +1,73 @@
+"""Pin the CPU oracle against the reference's own kernels (tests/golden, made by make_golden.py).
+
+The fixtures come from lbm3d.py's k_init / k_step / k_macro / k_accum bodies
+run in float32; the oracle evaluates the same expressions in the same order,
+so every field must match bit for bit, the never-written solid cells of the
+stale lattice included.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+
+@pytest.mark.parametrize("case", ["step_box", "step_rand"])
+def test_oracle_matches_reference_kernels(case, oracle_mod):
+    d = golden(case)
+    flag, uin = d["flag"], d["uin"]
+    nu0, cs, x_sponge, nu_sponge, noise, seed, n = d["params"]
+    f0 = oracle_mod.init(flag, uin, noise=np.float32(noise), seed=int(seed))
+    np.testing.assert_array_equal(f0, d["f_init"])
+    fa, fb = f0.copy(), np.zeros_like(f0)              # f1 starts as zeros (lbm3d.py:294)
+    for t in range(int(n)):
+        row = np.zeros((flag.shape[2], 2))
+        oracle_mod.step(fa, flag, uin, np.float32(nu0), np.float32(cs), int(x_sponge), np.float32(nu_sponge),
+                        f_out=fb, force_row=row)
+        fa, fb = fb, fa
+        np.testing.assert_array_equal(fa, d[f"f_step{t + 1}"])
+        np.testing.assert_array_equal(fb, d[f"f_other{t + 1}"])
+        np.testing.assert_allclose(row, d["force"][t], rtol=1e-12, atol=1e-15)
+    u = oracle_mod.macro(fa, flag)
+    np.testing.assert_array_equal(u, d["macro"])
+    acc = np.zeros(u.shape, np.float64)
+    oracle_mod.accum(u, acc)
+    oracle_mod.accum(u, acc)
+    np.testing.assert_array_equal(acc.astype(np.float32), d["accum2"])
+
+
+def test_oracle_tables_match_reference(oracle_mod):
+    d = golden("tables")
+    c, w, opp, mirz = oracle_mod.tables()
+    np.testing.assert_array_equal(c, d["C"])
+    np.testing.assert_array_equal(w, d["W"])
+    np.testing.assert_array_equal(opp, d["OPP"])
+    np.testing.assert_array_equal(mirz, d["MIRZ"])
+
+
+def test_oracle_f64_close_to_f32(oracle_mod):
+    """The float64 restatement follows the float32 one to float32 rounding."""
+    d = golden("step_box")
+    flag, uin = d["flag"], d["uin"]
+    nu0, cs, x_sponge, nu_sponge, noise, seed, n = d["params"]
+    f32, _ = oracle_mod.run(d["f_init"], flag, uin, np.float32(nu0), np.float32(cs), int(x_sponge), 3,
+                            np.float32(nu_sponge))
+    f64, _ = oracle_mod.run(d["f_init"].astype(np.float64), flag, uin, float(np.float32(nu0)),
+                            float(np.float32(cs)), int(x_sponge), 3, float(np.float32(nu_sponge)))
+    fluid = np.broadcast_to(flag == 0, f32.shape)
+    np.testing.assert_allclose(f32[fluid], f64[fluid], rtol=2e-6)
+
+
+def test_oracle_thread_count_invariance(oracle_mod):
+    """Forces and fields do not depend on the number of OpenMP threads."""
+    d = golden("step_rand")
+    flag, uin = d["flag"], d["uin"]
+    nu0, cs, x_sponge, nu_sponge, noise, seed, n = d["params"]
+    outs = []
+    nmax = oracle_mod.max_threads()
+    for nt in (1, max(2, nmax)):
+        oracle_mod.set_threads(nt)
+        outs.append(oracle_mod.run(d["f_init"], flag, uin, np.float32(nu0), np.float32(cs), int(x_sponge), 3,
+                                   np.float32(nu_sponge)))
+    oracle_mod.set_threads(nmax)
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
