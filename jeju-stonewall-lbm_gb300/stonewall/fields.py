@@ -99,13 +99,22 @@ class Flags:
         if f.shape != (grid.nx, grid.ny, grid.nz):
             raise ValueError(f"flag has shape {f.shape}, expected {(grid.nx, grid.ny, grid.nz)}")
         self.host = f
-        src = torch.from_numpy(f).to(device)
         self.flag = torch.empty(grid.cells_padded, dtype=torch.uint8, device=device)
         self.tiles = torch.empty(grid.tiles, dtype=torch.uint8, device=device)
-        s = _stream(stream)
-        N.check(N.lib().sw_pack_flag(grid.gp, _ptr(src), _ptr(self.flag), s), "sw_pack_flag")
-        N.check(N.lib().sw_build_tiles(grid.gp, _ptr(self.flag), _ptr(self.tiles), s), "sw_build_tiles")
+        self._ref = torch.empty((grid.nx, grid.ny, grid.nz), dtype=torch.uint8, device=device)
+        self.load(torch.from_numpy(f), stream=stream)
         (stream or torch.cuda.current_stream()).synchronize()
+
+    def load(self, flag_ref, stream=None):
+        """Copy flags (reference layout, host or device tensor; pinned host memory copies
+        asynchronously) into the device layout and reclassify the row segments."""
+        g = self.grid
+        if tuple(flag_ref.shape) != (g.nx, g.ny, g.nz) or flag_ref.dtype != torch.uint8:
+            raise ValueError(f"flag must be uint8 {(g.nx, g.ny, g.nz)}")
+        self._ref.copy_(flag_ref, non_blocking=True)
+        s = _stream(stream)
+        N.check(N.lib().sw_pack_flag(g.gp, _ptr(self._ref), _ptr(self.flag), s), "sw_pack_flag")
+        N.check(N.lib().sw_build_tiles(g.gp, _ptr(self.flag), _ptr(self.tiles), s), "sw_build_tiles")
 
     @property
     def ptr(self):

@@ -1,0 +1,225 @@
+"""WallSolver: one wall solve resident on the GPU, the public driver-level API.
+
+It owns what lbm3d.py:292-313 allocates (two lattices, flags, inlet, force
+series, the running mean) and replaces the time loop of lbm3d.py:358-370:
+each step is one fused k_step, and after the spin-up every 5th state is
+accumulated (k_macro + k_accum fused, sums in float64).  Runs of steps are
+replayed as CUDA graphs of `chunk` steps; the per-step force rows of a graph
+go to a ring buffer that is copied into the series after each replay, so one
+captured graph serves every chunk with the same ping-pong parity and
+accumulation phase.
+
+Checkpoints use the reference's directory format (lbm3d.py:342-355):
+f.npy (19, nx, ny, nz), force.npy (n_total, nz, 2), uacc.npy (4, nx, ny, nz),
+snaps_*.npy and state.json {t, n_acc, sig}, written to <dir>.tmp and swapped
+in once complete.  force and uacc are stored in float64 (the reference writes
+float32), which makes a resumed run bit-identical to an uninterrupted one;
+float32 files from the reference load as well.
+"""
+import json
+import os
+import shutil
+
+import numpy as np
+import torch
+
+from . import kernels as K
+from .fields import Accum, Flags, ForceSeries, Grid, Lattice, Macro
+
+
+class Diverged(RuntimeError):
+    pass
+
+
+class WallSolver:
+    def __init__(self, flag, uin, nu0, cs, x_sponge, n_total, n_spin=0, nu_sponge=0.05, dtype="f32",
+                 device="cuda", acc_every=5, chunk=50):
+        flag = np.asarray(flag, dtype=np.uint8)
+        nx, ny, nz = flag.shape
+        uin = np.asarray(uin, dtype=np.float32)
+        if uin.shape != (nz,):
+            raise ValueError(f"uin has shape {uin.shape}, expected ({nz},)")
+        self.device = torch.device(device)
+        self.grid = Grid(nx, ny, nz)
+        self.flags = Flags(self.grid, flag, device=self.device)
+        self.uin = K.DeviceVector(uin, device=self.device)
+        self.nu0, self.cs, self.x_sponge, self.nu_sponge = float(nu0), float(cs), int(x_sponge), float(nu_sponge)
+        self.n_total, self.n_spin, self.acc_every = int(n_total), int(n_spin), int(acc_every)
+        self.f = [Lattice(self.grid, dtype, device=self.device),
+                  Lattice(self.grid, dtype, device=self.device).zero_()]   # f1 = zeros, lbm3d.py:294
+        self.cur = 0
+        self.force = ForceSeries(self.n_total, nz, device=self.device)
+        self.acc = Accum(self.grid, device=self.device)
+        self.t = 0
+        self.n_acc = 0
+        self.chunk = int(chunk)
+        self._graphs = {}
+        self._ring = None
+        self.launches = 0          # kernels of this library launched by advance()
+
+    # ------------------------------------------------------------ state
+    @property
+    def state(self):
+        """The lattice holding the current populations (the reference's f0 after the swap)."""
+        return self.f[self.cur]
+
+    @property
+    def dtype(self):
+        return self.f[0].dtype
+
+    def memory_bytes(self):
+        g = self.grid
+        return (sum(f.nbytes for f in self.f) + self.flags.flag.numel() + self.flags.tiles.numel()
+                + self.force.data.numel() * 8 + self.acc.data.numel() * 8)
+
+    def reload(self, flag, uin):
+        """Start over with a new mask and inlet profile (torch tensors, pinned host memory copies
+        asynchronously): resets the step counter, forces and sums; keeps buffers and graphs."""
+        self.flags.load(flag)
+        if tuple(uin.shape) != (self.grid.nz,):
+            raise ValueError("uin has the wrong length")
+        self.uin.data.copy_(uin, non_blocking=True)
+        self.force.data.zero_()
+        self.acc.data.zero_()
+        self.t, self.n_acc, self.cur = 0, 0, 0
+        return self
+
+    def init(self, noise=0.02, seed=7, noise_kind="uniform"):
+        """k_init on the current lattice (lbm3d.py:340)."""
+        K.k_init(self.state, self.flags, self.uin, noise, seed, noise_kind)
+        return self
+
+    # ------------------------------------------------------------ stepping
+    def _step(self, force_rows, t_index):
+        src, dst = self.f[self.cur], self.f[1 - self.cur]
+        g = self.grid
+        K.k_step(src, dst, self.flags, self.uin, g.nx, g.ny, g.nz, self.nu0, self.cs, self.x_sponge,
+                 self.nu_sponge, force_rows, t_index)
+        self.cur ^= 1
+
+    def _accumulate_now(self, t):
+        return t >= self.n_spin and (t - self.n_spin) % self.acc_every == 0
+
+    def step(self):
+        """One eager step (lbm3d.py:359-370)."""
+        if self.t >= self.n_total:
+            raise RuntimeError("the run is complete")
+        self._step(self.force, self.t)
+        self.launches += 1
+        if self._accumulate_now(self.t):
+            K.k_macro_accum(self.state, self.flags, self.acc)
+            self.n_acc += 1
+            self.launches += 1
+        self.t += 1
+
+    def _graph_for(self, key):
+        if key in self._graphs:
+            return self._graphs[key]
+        n, cur0, phase = key
+        if self._ring is None or self._ring.n_steps != n:
+            self._ring = ForceSeries(n, self.grid.nz, device=self.device)
+        ring = self._ring
+        saved_cur = self.cur
+        self.cur = cur0
+        graph = torch.cuda.CUDAGraph()
+        # warm the capture path once on a side stream as torch recommends
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph):
+            ring.data.zero_()
+            for j in range(n):
+                self._step(ring, j)
+                if phase is not None and (phase + j) % self.acc_every == 0:
+                    K.k_macro_accum(self.state, self.flags, self.acc)
+        self.cur = saved_cur
+        n_acc = 0 if phase is None else sum(1 for j in range(n) if (phase + j) % self.acc_every == 0)
+        self._graphs[key] = (graph, n_acc)
+        return self._graphs[key]
+
+    def advance(self, n, use_graphs=True):
+        """Run n steps (graph-replayed in chunks where possible)."""
+        n = min(int(n), self.n_total - self.t)
+        c = self.chunk
+        while n > 0:
+            t = self.t
+            same_side = t >= self.n_spin or t + c <= self.n_spin
+            if use_graphs and n >= c and same_side:
+                phase = (t - self.n_spin) % self.acc_every if t >= self.n_spin else None
+                graph, n_acc = self._graph_for((c, self.cur, phase))
+                graph.replay()
+                self.force.data[t:t + c].copy_(self._ring.data)
+                self.cur ^= (c & 1)
+                self.t += c
+                self.n_acc += n_acc
+                self.launches += c + n_acc
+                n -= c
+            else:
+                self.step()
+                n -= 1
+        return self
+
+    def run(self, check_every=5000, log=None):
+        """Advance to n_total with a finiteness check every check_every steps (lbm3d.py:386-391)."""
+        while self.t < self.n_total:
+            nxt = min(self.n_total, (self.t // check_every + 1) * check_every)
+            self.advance(nxt - self.t)
+            self.check_finite()
+            if log:
+                log(self)
+        return self
+
+    # ------------------------------------------------------------ outputs
+    def macro(self):
+        """rho, ux, uy, uz of the current state in the reference layout (k_macro, lbm3d.py:367)."""
+        u = Macro(self.grid, device=self.device)
+        K.k_macro(self.state, self.flags, u)
+        return u.numpy()
+
+    def check_finite(self):
+        u = Macro(self.grid, device=self.device)
+        K.k_macro(self.state, self.flags, u)
+        if not bool(torch.isfinite(u.data).all()):
+            raise Diverged(f"diverged at step {self.t}")
+        return True
+
+    def force_series(self):
+        """(n_total, nz, 2) float64."""
+        return self.force.numpy()
+
+    def mean_field(self):
+        """Time-mean (rho, u) over the accumulated states, float64 (lbm3d.py:402)."""
+        return self.acc.numpy() / max(self.n_acc, 1)
+
+    # ------------------------------------------------------------ checkpoints
+    def save_checkpoint(self, path, sig, extra=None):
+        tmp = path + ".tmp"
+        if os.path.isdir(tmp):
+            shutil.rmtree(tmp)
+        os.makedirs(tmp)
+        ref_dtype = np.float64 if self.dtype == 1 else np.float32
+        np.save(os.path.join(tmp, "f.npy"), self.state.numpy(ref_dtype))
+        np.save(os.path.join(tmp, "force.npy"), self.force.numpy())
+        np.save(os.path.join(tmp, "uacc.npy"), self.acc.numpy())
+        g = self.grid
+        extra = extra or {}
+        np.save(os.path.join(tmp, "snaps_xz.npy"), extra.get("snaps_xz", np.zeros((0, 3, g.nx, g.nz), np.float16)))
+        np.save(os.path.join(tmp, "snaps_xy.npy"), extra.get("snaps_xy", np.zeros((0, 3, g.nx, g.ny), np.float16)))
+        np.save(os.path.join(tmp, "snaps_q.npy"), extra.get("snaps_q", np.zeros((0, 1, 1, 1), np.uint8)))
+        with open(os.path.join(tmp, "state.json"), "w") as fh:
+            json.dump(dict(t=self.t, n_acc=self.n_acc, sig=sig), fh)
+        if os.path.isdir(path):
+            shutil.rmtree(path)
+        os.replace(tmp, path)
+
+    def load_checkpoint(self, path, sig):
+        with open(os.path.join(path, "state.json")) as fh:
+            info = json.load(fh)
+        if info["sig"] != sig:
+            raise ValueError(f"checkpoint {path} was made with different settings")
+        self.t, self.n_acc = int(info["t"]), int(info["n_acc"])
+        self.cur = 0
+        self.f[0].assign(np.load(os.path.join(path, "f.npy")))
+        self.f[1].zero_()
+        self.force.assign(np.load(os.path.join(path, "force.npy")))
+        self.acc.assign(np.load(os.path.join(path, "uacc.npy")))
+        self._graphs.clear()
+        return info

@@ -1,0 +1,76 @@
+"""The C ABI library builds, loads and exports every function include/stonewall.h declares.
+
+CPU only: no call here launches device work.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "stonewall.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sw_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_kernel_entry_points():
+    names = declared_functions()
+    for must in ("sw_init", "sw_step", "sw_macro", "sw_accum", "sw_macro_accum", "sw_pack_f", "sw_unpack_f",
+                 "sw_build_tiles", "sw_geom_make"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    missing = [n for n in declared_functions() if not hasattr(native_lib, n)]
+    assert not missing, missing
+
+
+def test_host_only_entry_points(native_lib):
+    from stonewall import _native as N
+    assert b"sm_103a" in native_lib.sw_version()
+    g = N.geom(45, 7, 10)
+    assert (g.nx, g.ny, g.nz, g.pitch) == (45, 7, 10, 64)
+    assert native_lib.sw_cells_padded(ctypes.byref(g)) == 10 * 7 * 64
+    assert native_lib.sw_lattice_elems(ctypes.byref(g)) == 19 * 10 * 7 * 64
+    assert native_lib.sw_tile_count(ctypes.byref(g)) == 10 * 7 * 2
+    assert [native_lib.sw_dtype_size(d) for d in range(5)] == [4, 8, 2, 2, 0]
+    bad = N.SwGeom()
+    assert native_lib.sw_geom_make(0, 4, 4, ctypes.byref(bad)) == N.SW_ERR_BAD_ARG
+    assert native_lib.sw_geom_make(1 << 16, 1 << 16, 1 << 10, ctypes.byref(bad)) == N.SW_ERR_BAD_ARG
+    for s in range(7):
+        assert native_lib.sw_status_string(s)
+
+
+def test_entry_points_reject_bad_arguments_before_launching(native_lib):
+    """Argument checks run on the host: null pointers, bad dtype, aliasing, misalignment."""
+    from stonewall import _native as N
+    g = N.geom(32, 4, 4)
+    gp = ctypes.byref(g)
+    buf = np.zeros(64, np.uint8)
+    p = ctypes.c_void_p(buf.ctypes.data)
+    L = native_lib
+    assert L.sw_step(gp, 0, None, p, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None) == N.SW_ERR_BAD_ARG
+    assert L.sw_step(gp, 9, p, ctypes.c_void_p(buf.ctypes.data + 32), p, p, p, 0.0, 0.0, 0, 0.0, None, 0,
+                     None) == N.SW_ERR_BAD_ARG
+    assert L.sw_step(gp, 0, p, p, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None) == N.SW_ERR_BAD_ARG  # in place
+    assert L.sw_step(gp, 0, p, ctypes.c_void_p(buf.ctypes.data + 4), p, p, p, 0.0, 0.0, 0, 0.0, None, 0,
+                     None) == N.SW_ERR_BAD_ARG                                                    # misaligned
+    assert L.sw_init(gp, 0, p, p, p, 0.02, 1, 7, None) == N.SW_ERR_BAD_ARG                       # noise kind
+    assert L.sw_pack_f(gp, 0, 2, p, p, None) == N.SW_ERR_BAD_ARG                                  # ref dtype
+    assert L.sw_force_to_f64(None, None, -1, None) == N.SW_ERR_BAD_ARG
+
+
+def test_native_unavailable_is_loud(monkeypatch, tmp_path):
+    """With the library missing the package raises; there is no CPU fallback."""
+    from stonewall import _native as N
+    monkeypatch.setattr(N, "_lib", None)
+    monkeypatch.setattr(N, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(N.NativeUnavailable):
+        N.lib()
