@@ -42,7 +42,8 @@ enum {
   SW_ERR_NONFINITE = 3,   /* a non-finite density or velocity was found (sw_check_finite) */
   SW_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
   SW_ERR_CUDA = 5,        /* a CUDA call failed; sw_last_cuda_error() has the code */
-  SW_ERR_UNSUPPORTED = 6  /* valid request this build does not implement */
+  SW_ERR_UNSUPPORTED = 6, /* valid request this build does not implement */
+  SW_ERR_TOO_LARGE = 7    /* grid exceeds the fixed scratch of sw_step_noalloc */
 };
 
 /* storage type of the distributions */
@@ -129,6 +130,28 @@ int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *fl
 
 /* force rows (fixed point) -> double, n values. */
 int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s);
+
+/* ---------------------------------------------------------------- step without allocation
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory -- a host that only receives device pointers from an
+ * allocator it does not own, or a loop that must not call cudaMalloc/cudaFree
+ * because they can synchronise the device.  Same arguments and results as
+ * sw_step minus `tiles`: the row-segment classes live in a fixed device array
+ * of SW_NOALLOC_MAX_SEGMENTS bytes inside the library (every GPU that loads the
+ * library holds it until the process exits), rebuilt from `flag` on each call.
+ *   - grids with more than SW_NOALLOC_MAX_SEGMENTS segments (nz*ny*pitch/32,
+ *     about 134 M cells) are rejected with SW_ERR_TOO_LARGE;
+ *   - nothing is allocated, neither by the library nor by the CUDA runtime on
+ *     its behalf;
+ *   - the first call on a device looks up the array's device address (once per
+ *     device, with that device current): make that first call before any
+ *     stream capture;
+ *   - all calls on a device share the array: calls that overlap on the GPU
+ *     (other streams, other host threads) race and must be serialised. */
+#define SW_NOALLOC_MAX_SEGMENTS (1 << 22)
+int sw_step_noalloc(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
+                    const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
+                    int64_t t, sw_stream s);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,8 @@ cudaError_t aux_unpack_acc(const Geom &g, const double *acc, double *ref, cudaSt
 cudaError_t aux_build_tiles(const Geom &g, const uint8_t *flag, uint8_t *tiles, cudaStream_t s);
 cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cudaStream_t s);
 
+int note_cuda_error(int cuda_error);  // sw_capi.cu
+
 // one launcher per storage type, each in its own translation unit (sw_step_<dtype>.cu)
 cudaError_t step_f32(const StepParams &p, cudaStream_t s);
 cudaError_t step_f64(const StepParams &p, cudaStream_t s);

@@ -42,6 +42,12 @@ cudaStream_t st(sw_stream s) { return reinterpret_cast<cudaStream_t>(s); }
 
 }  // namespace
 
+namespace sw {
+// Records a CUDA error code for sw_last_cuda_error() and returns SW_ERR_CUDA
+// (for entry points defined in other translation units).
+int note_cuda_error(int cuda_error) { return cuda_status((cudaError_t)cuda_error); }
+}  // namespace sw
+
 extern "C" {
 
 const char *sw_version(void) { return "stonewall-gb300 0.1 (sm_103a)"; }
@@ -55,6 +61,7 @@ const char *sw_status_string(int status) {
     case SW_ERR_TIMEOUT: return "device wait timed out";
     case SW_ERR_CUDA: return "CUDA error";
     case SW_ERR_UNSUPPORTED: return "unsupported";
+    case SW_ERR_TOO_LARGE: return "grid larger than the fixed scratch of sw_step_noalloc";
     default: return "unknown status";
   }
 }
