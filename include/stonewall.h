@@ -120,6 +120,27 @@ int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const ui
             const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge,
             double nu_sponge, int64_t *force, int64_t t, sw_stream s);
 
+/* k_step followed by k_macro + k_accum of the new state (lbm3d.py:359-369 on an
+ * accumulation step) in one pass: as sw_step, and (rho, ux, uy, uz) of every
+ * fluid cell is added to acc (float64, [4][nz][ny][pitch]).  Non-fluid cells of
+ * acc are not touched (their sums are n_acc * (1, 0, 0, 0) by definition). */
+int sw_step_accum(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
+                  const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge,
+                  double nu_sponge, int64_t *force, int64_t t, double *acc, sw_stream s);
+
+/* Launch configurations of the step (block shape and register budget, see
+ * csrc/sw_step.cuh).  sw_step and sw_step_accum use the configuration set for
+ * their storage type (process-wide, default 0); stonewall/autotune.py times
+ * every configuration with sw_step_cfg and sets the fastest.  No reference
+ * counterpart (Warp chooses its own launch shape). */
+int sw_step_config_count(void);
+int sw_set_step_config(int dtype, int cfg);
+int sw_get_step_config(int dtype);
+/* sw_step (acc NULL) or sw_step_accum (acc non-NULL) with an explicit configuration. */
+int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
+                const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge,
+                int64_t *force, int64_t t, double *acc, int cfg, sw_stream s);
+
 /* k_macro, lbm3d.py:158-182 (lbm3d.py:367, 387): u = (rho, ux, uy, uz); solids -> (1, 0, 0, 0). */
 int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s);
 /* k_accum, lbm3d.py:185-188 (lbm3d.py:369): acc += u, in double. */

@@ -129,10 +129,15 @@ int sw_init(const sw_geom *g, int dtype, void *f, const uint8_t *flag, const flo
   return cuda_status(sw::aux_init(to_geom(g), dtype, f, flag, uin, noise, seed, noise_kind, st(s)));
 }
 
-int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
-            const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force, int64_t t,
-            sw_stream s) {
+namespace {
+// launch configuration used by sw_step / sw_step_accum, per storage type
+int g_step_cfg[4] = {0, 0, 0, 0};
+
+int step_impl(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
+              const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
+              int64_t t, double *acc, int cfg, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f_in || !f_out || !flag || !tiles || !uin) return SW_ERR_BAD_ARG;
+  if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
   if (f_in == f_out || !aligned16(f_in) || !aligned16(f_out) || t < 0) return SW_ERR_BAD_ARG;
   sw::StepParams p;
   p.fin = f_in;
@@ -145,7 +150,10 @@ int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const ui
   p.cs = cs;
   p.nu_sponge = nu_sponge;
   p.x_sponge = x_sponge;
+  p.sponge_scale = (g->nx != x_sponge) ? 1.0 / (double)(g->nx - x_sponge) : 0.0;
   p.force = force ? reinterpret_cast<long long *>(force) + (size_t)t * 2 * g->nz : nullptr;
+  p.acc = acc;
+  p.cfg = cfg;
   cudaError_t e;
   switch (dtype) {
     case SW_F32: e = sw::step_f32(p, st(s)); break;
@@ -155,6 +163,38 @@ int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const ui
   }
   return cuda_status(e);
 }
+}  // namespace
+
+int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
+            const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force, int64_t t,
+            sw_stream s) {
+  return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, nullptr,
+                   dtype_ok(dtype) ? g_step_cfg[dtype] : 0, s);
+}
+
+int sw_step_accum(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
+                  const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge,
+                  int64_t *force, int64_t t, double *acc, sw_stream s) {
+  if (!acc) return SW_ERR_BAD_ARG;
+  return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, acc,
+                   dtype_ok(dtype) ? g_step_cfg[dtype] : 0, s);
+}
+
+int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
+                const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
+                int64_t t, double *acc, int cfg, sw_stream s) {
+  return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, acc, cfg, s);
+}
+
+int sw_step_config_count(void) { return sw::kStepConfigs; }
+
+int sw_set_step_config(int dtype, int cfg) {
+  if (!dtype_ok(dtype) || cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
+  g_step_cfg[dtype] = cfg;
+  return SW_OK;
+}
+
+int sw_get_step_config(int dtype) { return dtype_ok(dtype) ? g_step_cfg[dtype] : -1; }
 
 int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !u) return SW_ERR_BAD_ARG;

@@ -64,15 +64,17 @@ constexpr double FORCE_SCALE = 1099511627776.0;  // 2^40
 
 // ---------------------------------------------------------------- storage policies
 // R = arithmetic type of the collision, T = stored type.  The shifted 16-bit
-// formats store f_i - w_i (the deviation from the rest state) to keep the
-// significant bits where the signal is.
+// formats store g_i = f_i - w_i (the deviation from the rest state) to keep the
+// significant bits where the signal is, and the step computes on g directly
+// (kShift): ld / st move values of the compute domain (g when shifted, f
+// otherwise); enc / dec convert full f values (init, layout transposes, macro).
 template <int DT> struct Store;
 
 template <> struct Store<SW_F32> {
   using T = float;
   using R = float;
+  static constexpr bool kShift = false;
   template <int I> static __device__ __forceinline__ R ld(const T *p) { return __ldg(p); }
-  template <int I> static __device__ __forceinline__ R ld_rw(const T *p) { return *p; }
   template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, v); }
   template <int I> static __device__ __forceinline__ T enc(R v) { return v; }
   template <int I> static __device__ __forceinline__ R dec(T v) { return v; }
@@ -80,8 +82,8 @@ template <> struct Store<SW_F32> {
 template <> struct Store<SW_F64> {
   using T = double;
   using R = double;
+  static constexpr bool kShift = false;
   template <int I> static __device__ __forceinline__ R ld(const T *p) { return __ldg(p); }
-  template <int I> static __device__ __forceinline__ R ld_rw(const T *p) { return *p; }
   template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, v); }
   template <int I> static __device__ __forceinline__ T enc(R v) { return v; }
   template <int I> static __device__ __forceinline__ R dec(T v) { return v; }
@@ -89,20 +91,20 @@ template <> struct Store<SW_F64> {
 template <> struct Store<SW_F16_SHIFT> {
   using T = __half;
   using R = float;
+  static constexpr bool kShift = true;
   template <int I> static __device__ __forceinline__ R dec(T v) { return W<float>(I) + __half2float(v); }
   template <int I> static __device__ __forceinline__ T enc(R v) { return __float2half_rn(v - W<float>(I)); }
-  template <int I> static __device__ __forceinline__ R ld(const T *p) { return dec<I>(__ldg(p)); }
-  template <int I> static __device__ __forceinline__ R ld_rw(const T *p) { return dec<I>(*p); }
-  template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, enc<I>(v)); }
+  template <int I> static __device__ __forceinline__ R ld(const T *p) { return __half2float(__ldg(p)); }
+  template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, __float2half_rn(v)); }
 };
 template <> struct Store<SW_BF16_SHIFT> {
   using T = __nv_bfloat16;
   using R = float;
+  static constexpr bool kShift = true;
   template <int I> static __device__ __forceinline__ R dec(T v) { return W<float>(I) + __bfloat162float(v); }
   template <int I> static __device__ __forceinline__ T enc(R v) { return __float2bfloat16_rn(v - W<float>(I)); }
-  template <int I> static __device__ __forceinline__ R ld(const T *p) { return dec<I>(__ldg(p)); }
-  template <int I> static __device__ __forceinline__ R ld_rw(const T *p) { return dec<I>(*p); }
-  template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, enc<I>(v)); }
+  template <int I> static __device__ __forceinline__ R ld(const T *p) { return __bfloat162float(__ldg(p)); }
+  template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, __float2bfloat16_rn(v)); }
 };
 
 // lbm3d.py:33-36, same evaluation order.

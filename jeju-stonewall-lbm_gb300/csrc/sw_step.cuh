@@ -1,18 +1,31 @@
 // sw_step.cuh -- the fused D3Q19 timestep (pull streaming + boundaries + bounce-back +
 // momentum exchange + regularized BGK with Smagorinsky and the outlet sponge).
 //
-// Follows k_step of stonewall3d/lbm3d.py:57-155 term by term.  Differences in
-// form, none in result beyond floating-point contraction:
+// Computes k_step of stonewall3d/lbm3d.py:57-155.  Same mathematics, arranged
+// for the GPU:
 //  * one warp = one 32-cell row segment along x; a byte per segment (tiles[])
-//    says whether any pull source can be non-fluid.  Segments that cannot
-//    (the bulk of the domain) skip the 19 neighbour flag loads of
-//    lbm3d.py:88 and the force bookkeeping;
-//  * products with a zero lattice component (v * 0, lbm3d.py:119-127, 153-154)
-//    are skipped: for finite values they add +-0 and change nothing;
-//  * the per-cell wall force is summed per warp in float64 (xor butterfly,
-//    fixed order) and added to force[t][z] as 2^-40 fixed point with one
-//    64-bit integer atomic per warp, so the totals are independent of warp
-//    scheduling (the reference adds float32 atomics per cell, lbm3d.py:99-101).
+//    says whether any pull source of its fluid cells can be non-fluid.
+//    Segments that cannot (the bulk of the domain) skip the 19 neighbour flag
+//    loads of lbm3d.py:88 and the force bookkeeping;
+//  * the 18 moving populations are taken in opposite pairs (i, opp(i)):
+//    s = f_i + f_opp, d = f_i - f_opp give rho, momentum m and the second
+//    moment Pi with one add per term, and the regularized post-collision state
+//      f_i = w_i [rho + 3 c_i.m + 4.5 Q_i:B],  B = m m / rho + (1 - 1/tau) Pi_neq,
+//    Q_i = c_i c_i - I/3, is the reference's feq_i + (1 - 1/tau) w_i 4.5 Q_i:Pi_neq
+//    (lbm3d.py:147-155) rewritten: both members of a pair share w (rho + 4.5 Q:B)
+//    and differ in the sign of 3 w c.m.  Results agree with the reference's
+//    expression order to float32 rounding (the parity tests bound it at 1e-5);
+//  * one reciprocal of rho and one of tau replace the divisions;
+//  * the per-cell wall force (float32, as lbm3d.py:91-95) is summed per warp in
+//    float64 (xor butterfly, fixed order) and added to force[t][z] as 2^-40
+//    fixed point with one 64-bit integer atomic per warp, so the totals do not
+//    depend on warp scheduling (the reference adds float32 atomics per cell,
+//    lbm3d.py:99-101);
+//  * on accumulation steps (ACC) the cell's (rho, u) is added to the float64
+//    running sums in the same pass: this is k_macro + k_accum (lbm3d.py:367-369)
+//    of the new state, whose rho and m equal the pulled ones (the collision
+//    conserves both).  Non-fluid cells are not touched; their sums are
+//    n_acc * (1, 0, 0, 0) by definition and are filled in on download.
 #pragma once
 #include "sw_common.cuh"
 
@@ -26,83 +39,122 @@ struct StepParams {
   const float *uin;
   Geom g;
   double nu0, cs, nu_sponge;
+  double sponge_scale;  // 1 / (nx - x_sponge)
   int x_sponge;
   long long *force;  // force row of this step: [nz][2], or nullptr
+  double *acc;       // float64 running sums [4][plane] (accumulation steps only)
+  int cfg;           // launch configuration (SW_STEP_CONFIGS)
 };
 
-// Regularized-BGK collision of one cell from its 19 pulled populations fl[],
-// lbm3d.py:103-155.  Writes f_out through `put(Int<i>, value)`.
-template <typename R, typename Put>
-__device__ __forceinline__ void collide(const R (&fl)[Q], int x, const Geom &g, R nu0, R cs, int x_sponge,
-                                        R nu_sponge, Put &&put) {
-  R rho = R(0.0), mx = R(0.0), my = R(0.0), mz = R(0.0);
-  R pxx = R(0.0), pyy = R(0.0), pzz = R(0.0), pxy = R(0.0), pxz = R(0.0), pyz = R(0.0);
-  static_for<0, Q>([&](auto I) {
-    constexpr int i = decltype(I)::value;
-    constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
-    const R v = fl[i];
-    rho += v;
-    if constexpr (ex != 0) mx += (ex > 0 ? v : -v);
-    if constexpr (ey != 0) my += (ey > 0 ? v : -v);
-    if constexpr (ez != 0) mz += (ez > 0 ? v : -v);
-    if constexpr (ex != 0) pxx += v;
-    if constexpr (ey != 0) pyy += v;
-    if constexpr (ez != 0) pzz += v;
-    if constexpr (ex * ey != 0) pxy += (ex * ey > 0 ? v : -v);
-    if constexpr (ex * ez != 0) pxz += (ex * ez > 0 ? v : -v);
-    if constexpr (ey * ez != 0) pyz += (ey * ez > 0 ? v : -v);
-  });
-  const R ux = mx / rho, uy = my / rho, uz = mz / rho;
-  const R third = rho / R(3.0);
-  const R nxx = pxx - third - rho * ux * ux;
-  const R nyy = pyy - third - rho * uy * uy;
-  const R nzz = pzz - third - rho * uz * uz;
-  const R nxy = pxy - rho * ux * uy;
-  const R nxz = pxz - rho * ux * uz;
-  const R nyz = pyz - rho * uy * uz;
+__device__ __forceinline__ float rcp(float v) { return __frcp_rn(v); }
+__device__ __forceinline__ double rcp(double v) { return 1.0 / v; }
+
+// Regularized-BGK collision of one cell from its 19 pulled populations.
+// Calls put(Int<i>, value) for every population and returns rho and u.
+// SHIFT: f[] holds g_i = f_i - w_i and put() receives g_i.  Since sum_i w_i = 1,
+// sum_i w_i c_i = 0 and sum_i w_i c_i c_i = I/3, the moments of g are rho - 1,
+// m and Pi - I/3, so r0 = sum_i f[i] below is rho - 1 (shifted) or rho, and
+// Pi_neq = P - r0/3 I - m m / rho holds in both cases.
+template <typename R, bool SHIFT, typename Put>
+__device__ __forceinline__ void collide(const R (&f)[Q], int x, R nu0, R cs2_18r2, int x_sponge, R sponge_scale,
+                                        R nu_sponge, R &rho_out, R &ux_out, R &uy_out, R &uz_out, Put &&put) {
+  // pair sums / differences, pair k = directions (2k+1, 2k+2), c(2k+2) = -c(2k+1)
+  R s[9], d[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    s[k] = f[2 * k + 1] + f[2 * k + 2];
+    d[k] = f[2 * k + 1] - f[2 * k + 2];
+  }
+  // pairs: 0 (1,0,0) 1 (0,1,0) 2 (0,0,1) 3 (1,1,0) 4 (1,-1,0) 5 (1,0,1) 6 (1,0,-1) 7 (0,1,1) 8 (0,1,-1)
+  const R r0 = f[0] + (((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7])) + s[8]);
+  const R rho = SHIFT ? r0 + R(1.0) : r0;
+  const R mx = (d[0] + d[3]) + (d[4] + d[5]) + d[6];
+  const R my = (d[1] + d[3]) - d[4] + (d[7] + d[8]);
+  const R mz = (d[2] + d[5]) - d[6] + (d[7] - d[8]);
+  const R pxx = (s[0] + s[3]) + (s[4] + s[5]) + s[6];
+  const R pyy = (s[1] + s[3]) + (s[4] + s[7]) + s[8];
+  const R pzz = (s[2] + s[5]) + (s[6] + s[7]) + s[8];
+  const R pxy = s[3] - s[4];
+  const R pxz = s[5] - s[6];
+  const R pyz = s[7] - s[8];
+  const R inv = rcp(rho);
+  const R ux = mx * inv, uy = my * inv, uz = mz * inv;
+  const R third = r0 * R(1.0 / 3.0);
+  // non-equilibrium stress (lbm3d.py:133-138)
+  const R nxx = pxx - third - mx * ux;
+  const R nyy = pyy - third - my * uy;
+  const R nzz = pzz - third - mz * uz;
+  const R nxy = pxy - mx * uy;
+  const R nxz = pxz - mx * uz;
+  const R nyz = pyz - my * uz;
+  // sponge viscosity (lbm3d.py:140-143) and Smagorinsky time scale (lbm3d.py:144-147)
   R nu = nu0;
   if (x > x_sponge) {
-    const R s = R(x - x_sponge) / R(g.nx - x_sponge);
-    nu = nu0 + nu_sponge * s * s;
+    const R sp = R(x - x_sponge) * sponge_scale;
+    nu = nu0 + nu_sponge * sp * sp;
   }
   const R tau0 = R(3.0) * nu + R(0.5);
   const R qn = sqrt(nxx * nxx + nyy * nyy + nzz * nzz + R(2.0) * (nxy * nxy + nxz * nxz + nyz * nyz));
-  const R tau = R(0.5) * (tau0 + sqrt(tau0 * tau0 + R(18.0) * sqrt(R(2.0)) * cs * cs * qn / rho));
-  const R keep = R(1.0) - R(1.0) / tau;
-  const R usq = ux * ux + uy * uy + uz * uz;
-  static_for<0, Q>([&](auto I) {
-    constexpr int i = decltype(I)::value;
-    constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
-    constexpr R third_c = R(1.0) / R(3.0);
-    constexpr R kx = R(ex * ex) - third_c, ky = R(ey * ey) - third_c, kz = R(ez * ez) - third_c;
-    R off = R(0.0);
-    if constexpr (ex * ey != 0) off += (ex * ey > 0 ? nxy : -nxy);
-    if constexpr (ex * ez != 0) off += (ex * ez > 0 ? nxz : -nxz);
-    if constexpr (ey * ez != 0) off += (ey * ez > 0 ? nyz : -nyz);
-    const R qq = kx * nxx + ky * nyy + kz * nzz + R(2.0) * off;
-    R cu = R(0.0);
-    if constexpr (ex != 0) cu += (ex > 0 ? ux : -ux);
-    if constexpr (ey != 0) cu += (ey > 0 ? uy : -uy);
-    if constexpr (ez != 0) cu += (ez > 0 ? uz : -uz);
-    cu = R(3.0) * cu;
-    const R feq = W<R>(i) * rho * (R(1.0) + cu + R(0.5) * cu * cu - R(1.5) * usq);
-    put(Int<i>{}, feq + keep * W<R>(i) * R(4.5) * qq);
-  });
+  const R tau = R(0.5) * (tau0 + sqrt(tau0 * tau0 + cs2_18r2 * qn * inv));
+  const R keep = R(1.0) - rcp(tau);
+  // B = rho u u + keep Pi_neq and the pair terms of Q_i : B
+  const R bxx = mx * ux + keep * nxx, byy = my * uy + keep * nyy, bzz = mz * uz + keep * nzz;
+  const R bxy2 = R(2.0) * (mx * uy + keep * nxy);
+  const R bxz2 = R(2.0) * (mx * uz + keep * nxz);
+  const R byz2 = R(2.0) * (my * uz + keep * nyz);
+  const R tr = (bxx + byy + bzz) * R(1.0 / 3.0);
+  const R w0 = W<R>(0), w1 = W<R>(1), w2 = W<R>(7);
+  put(Int<0>{}, w0 * (r0 - R(4.5) * tr));
+  auto pair = [&](auto I, R w, R qb, R cm) {
+    constexpr int k = decltype(I)::value;
+    const R base = w * (r0 + R(4.5) * qb);
+    const R anti = (R(3.0) * w) * cm;
+    put(Int<2 * k + 1>{}, base + anti);
+    put(Int<2 * k + 2>{}, base - anti);
+  };
+  pair(Int<0>{}, w1, bxx - tr, mx);
+  pair(Int<1>{}, w1, byy - tr, my);
+  pair(Int<2>{}, w1, bzz - tr, mz);
+  const R exy = bxx + byy - tr, exz = bxx + bzz - tr, eyz = byy + bzz - tr;
+  pair(Int<3>{}, w2, exy + bxy2, mx + my);
+  pair(Int<4>{}, w2, exy - bxy2, mx - my);
+  pair(Int<5>{}, w2, exz + bxz2, mx + mz);
+  pair(Int<6>{}, w2, exz - bxz2, mx - mz);
+  pair(Int<7>{}, w2, eyz + byz2, my + mz);
+  pair(Int<8>{}, w2, eyz - byz2, my - mz);
+  rho_out = rho;
+  ux_out = ux;
+  uy_out = uy;
+  uz_out = uz;
 }
 
+// Launch configurations compiled in; the autotuner (stonewall/autotune.py)
+// times them per storage type and grid and keeps the fastest.
+//   WY   rows of a block (one 32-cell segment per warp): block = 32 x WY threads
+//   MINB resident blocks per SM asked of the register allocator
+template <int WY_, int MINB_> struct StepCfg {
+  static constexpr int WY = WY_;
+  static constexpr int MINB = MINB_;
+  static constexpr int THREADS = 32 * WY_;
+};
+#define SW_STEP_CONFIGS(X) X(0, 8, 4) X(1, 8, 5) X(2, 4, 8) X(3, 4, 12)
+constexpr int kStepConfigs = 4;
+
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
-// tests (segments next to stones, the ground or a fluid cell at z = 0).
-template <int DT, bool CHECK>
+// tests (segments next to stones, the ground or a fluid cell at z = 0).  Idx is
+// the type of element offsets into a lattice: int when 19 planes fit in 2^31
+// elements (every grid up to 113 M cells), long long otherwise.
+template <int DT, bool CHECK, bool ACC, typename Idx>
 __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int z, typename Store<DT>::R &fxw,
                                           typename Store<DT>::R &fzw, int &hit) {
   using S = Store<DT>;
   using T = typename S::T;
   using R = typename S::R;
   const Geom &g = p.g;
+  const Idx plane = (Idx)g.plane;
+  const int c = (z * g.ny + y) * g.pitch + x;
   const T *__restrict__ fin = static_cast<const T *>(p.fin);
   T *__restrict__ fout = static_cast<T *>(p.fout);
-  const size_t plane = (size_t)g.plane;
-  const unsigned c = ((unsigned)z * g.ny + y) * g.pitch + x;
   if (CHECK && p.flag[c] != 0) return;                          // lbm3d.py:65-66
   if (x == 0) {                                                 // inlet, lbm3d.py:67-71
     const R u0 = (R)__ldg(p.uin + z);
@@ -114,24 +166,30 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
       if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
       cu = R(3.0) * cu;
       const R v = W<R>(i) * R(1.0) * (R(1.0) + cu + R(0.5) * cu * cu - R(1.5) * usq);
-      S::template st<i>(fout + (size_t)i * plane + c, v);
+      S::template st<i>(fout + ((Idx)i * plane + c), S::kShift ? v - W<R>(i) : v);
     });
+    if (ACC) {
+      atomicAdd(p.acc + c, 1.0);
+      atomicAdd(p.acc + ((Idx)plane + c), (double)u0);
+    }
     return;
   }
-  // pull sources (lbm3d.py:77-86): periodic y, outlet copies column x, top mirrors z
-  const int ym = (y == 0) ? g.ny - 1 : y - 1;    // source row of c_y = +1
-  const int yp = (y == g.ny - 1) ? 0 : y + 1;    // source row of c_y = -1
+  // pull sources (lbm3d.py:77-86) as element offsets from the cell:
+  // periodic y, outlet copies column x, top mirrors z
+  const int row = g.pitch, lev = g.ny * g.pitch;
+  const int off_xm = c - 1;                                         // source of c_x = +1
+  const int off_xp = (x + 1 >= g.nx) ? c : c + 1;                   // source of c_x = -1
+  const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;            // source row of c_y = +1
+  const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;     // source row of c_y = -1
   const bool top = (z == g.nz - 1);
-  const int zp = top ? z : z + 1;                // source level of c_z = -1
-  const int xp = (x + 1 >= g.nx) ? x : x + 1;    // source column of c_x = -1
+  const int off_zm = -lev;                                          // source level of c_z = +1
+  const int off_zp = top ? 0 : lev;                                 // source level of c_z = -1
   R fl[Q];
   static_for<0, Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
     constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
-    const int xs = ex == 1 ? x - 1 : (ex == -1 ? xp : x);
-    const int ys = ey == 1 ? ym : (ey == -1 ? yp : y);
-    const int zs = ez == 1 ? z - 1 : (ez == -1 ? zp : z);
-    const unsigned src = ((unsigned)zs * g.ny + ys) * g.pitch + xs;
+    const int src = (ex == 1 ? off_xm : ex == -1 ? off_xp : c) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
+                    (ez == 1 ? off_zm : ez == -1 ? off_zp : 0);
     bool pull = true;
     if constexpr (CHECK) {
       // a source below z = 0 (only for a fluid cell in the bottom plane, which
@@ -139,9 +197,9 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
       const uint8_t fs = (ez == 1 && z == 0) ? (uint8_t)SW_GROUND : __ldg(p.flag + src);
       if (fs != 0) {                                            // lbm3d.py:89-95
         pull = false;
-        const R val = S::template ld<OPP(i)>(fin + (size_t)OPP(i) * plane + c);
+        const R val = S::template ld<OPP(i)>(fin + ((Idx)OPP(i) * plane + c));
         if (fs == SW_WALL) {
-          const R fr = val - W<R>(i);
+          const R fr = S::kShift ? val : val - W<R>(i);   // f - w, the rho = 1 background removed
           if constexpr (ex != 0) fxw = fxw - R(2.0) * fr * R(ex);
           if constexpr (ez != 0) fzw = fzw - R(2.0) * fr * R(ez);
           hit = 1;
@@ -151,42 +209,49 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
     }
     if (pull) {                                                 // lbm3d.py:97
       if constexpr (ez == -1) {
-        if (top) fl[i] = S::template ld<MIRZ(i)>(fin + (size_t)MIRZ(i) * plane + src);
-        else fl[i] = S::template ld<i>(fin + (size_t)i * plane + src);
+        if (top) fl[i] = S::template ld<MIRZ(i)>(fin + ((Idx)MIRZ(i) * plane + src));
+        else fl[i] = S::template ld<i>(fin + ((Idx)i * plane + src));
       } else {
-        fl[i] = S::template ld<i>(fin + (size_t)i * plane + src);
+        fl[i] = S::template ld<i>(fin + ((Idx)i * plane + src));
       }
     }
   });
-  collide<R>(fl, x, g, (R)p.nu0, (R)p.cs, p.x_sponge, (R)p.nu_sponge, [&](auto I, R v) {
-    constexpr int i = decltype(I)::value;
-    S::template st<i>(fout + (size_t)i * plane + c, v);
-  });
+  R rho, ux, uy, uz;
+  const R cs = (R)p.cs;
+  collide<R, S::kShift>(fl, x, (R)p.nu0, R(18.0) * sqrt(R(2.0)) * cs * cs, p.x_sponge, (R)p.sponge_scale,
+                        (R)p.nu_sponge, rho, ux, uy, uz, [&](auto I, R v) {
+                          constexpr int i = decltype(I)::value;
+                          S::template st<i>(fout + ((Idx)i * plane + c), v);
+                        });
+  if (ACC) {  // each cell is owned by one thread: reductions without a return value (no read stall)
+    double *a = p.acc;
+    atomicAdd(a + c, (double)rho);
+    atomicAdd(a + ((Idx)plane + c), (double)ux);
+    atomicAdd(a + ((Idx)2 * plane + c), (double)uy);
+    atomicAdd(a + ((Idx)3 * plane + c), (double)uz);
+  }
 }
 
-constexpr int STEP_THREADS = 256;
-constexpr int STEP_WARPS = STEP_THREADS / 32;
-
-template <int DT>
-__global__ void __launch_bounds__(STEP_THREADS) k_step_pull(StepParams p) {
+// Grid: (pitch / 32, ceil(ny / WY), nz); warp (threadIdx.y) = one row segment.
+template <int DT, bool ACC, typename Idx, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(StepParams p) {
   using R = typename Store<DT>::R;
-  const int seg = blockIdx.x * STEP_WARPS + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
   const Geom &g = p.g;
-  if (seg >= g.nseg_x * g.ny * g.nz) return;
+  const int y = blockIdx.y * Cfg::WY + threadIdx.y;
+  if (y >= g.ny) return;
+  const int z = blockIdx.z;
+  const int lane = threadIdx.x;
+  const int seg = (z * g.ny + y) * g.nseg_x + blockIdx.x;
   const uint8_t kind = __ldg(p.tiles + seg);
   if (kind & TILE_ALL_SOLID) return;
-  const int sx = seg % g.nseg_x;
-  const int row = seg / g.nseg_x;
-  const int y = row % g.ny, z = row / g.ny;
-  const int x = sx * SEG + lane;
+  const int x = blockIdx.x * SEG + lane;
   R fxw = R(0.0), fzw = R(0.0);
   int hit = 0;
   if (!(kind & TILE_CHECK)) {
-    if (x < g.nx) step_cell<DT, false>(p, x, y, z, fxw, fzw, hit);
+    if (x < g.nx) step_cell<DT, false, ACC, Idx>(p, x, y, z, fxw, fzw, hit);
     return;
   }
-  if (x < g.nx) step_cell<DT, true>(p, x, y, z, fxw, fzw, hit);
+  if (x < g.nx) step_cell<DT, true, ACC, Idx>(p, x, y, z, fxw, fzw, hit);
   if ((kind & TILE_FORCE) && p.force != nullptr) {              // lbm3d.py:99-101
     double dx = (double)fxw, dz = (double)fzw;
     const unsigned any = __ballot_sync(0xffffffffu, hit);
@@ -204,12 +269,34 @@ __global__ void __launch_bounds__(STEP_THREADS) k_step_pull(StepParams p) {
   }
 }
 
+template <int DT, bool ACC, typename Idx, typename Cfg>
+cudaError_t launch_cfg(const StepParams &p, cudaStream_t s) {
+  const dim3 grid((unsigned)p.g.nseg_x, (unsigned)((p.g.ny + Cfg::WY - 1) / Cfg::WY), (unsigned)p.g.nz);
+  const dim3 block(32, Cfg::WY);
+  k_step_pull<DT, ACC, Idx, Cfg><<<grid, block, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+// Narrow grids (19 planes < 2^31 elements) run the chosen configuration;
+// wider ones run configuration 0 with 64-bit offsets.
 template <int DT>
 cudaError_t launch_step(const StepParams &p, cudaStream_t s) {
-  const long long nseg = (long long)p.g.nseg_x * p.g.ny * p.g.nz;
-  const long long blocks = (nseg + STEP_WARPS - 1) / STEP_WARPS;
-  k_step_pull<DT><<<(unsigned)blocks, STEP_THREADS, 0, s>>>(p);
-  return cudaGetLastError();
+  const bool narrow = (long long)Q * p.g.plane < (1ll << 31);
+  if (p.g.nz > 65535) return cudaErrorInvalidValue;
+  if (!narrow) {
+    using C0 = StepCfg<8, 4>;
+    return p.acc ? launch_cfg<DT, true, long long, C0>(p, s) : launch_cfg<DT, false, long long, C0>(p, s);
+  }
+  switch (p.cfg) {
+#define SW_CASE(ID, WY, MINB)                                                                      \
+  case ID:                                                                                         \
+    return p.acc ? launch_cfg<DT, true, int, StepCfg<WY, MINB>>(p, s)                             \
+                 : launch_cfg<DT, false, int, StepCfg<WY, MINB>>(p, s);
+    SW_STEP_CONFIGS(SW_CASE)
+#undef SW_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace sw

@@ -81,6 +81,12 @@ def lib():
         "sw_build_tiles": ([G, P, P, P], ctypes.c_int),
         "sw_init": ([G, ctypes.c_int, P, P, P, f32, i32, i32, P], ctypes.c_int),
         "sw_step": ([G, ctypes.c_int, P, P, P, P, P, f64, f64, i32, f64, P, i64, P], ctypes.c_int),
+        "sw_step_accum": ([G, ctypes.c_int, P, P, P, P, P, f64, f64, i32, f64, P, i64, P, P], ctypes.c_int),
+        "sw_step_cfg": ([G, ctypes.c_int, P, P, P, P, P, f64, f64, i32, f64, P, i64, P, ctypes.c_int, P],
+                        ctypes.c_int),
+        "sw_step_config_count": ([], ctypes.c_int),
+        "sw_set_step_config": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "sw_get_step_config": ([ctypes.c_int], ctypes.c_int),
         "sw_macro": ([G, ctypes.c_int, P, P, P, P], ctypes.c_int),
         "sw_accum": ([G, P, P, P], ctypes.c_int),
         "sw_macro_accum": ([G, ctypes.c_int, P, P, P, P, P], ctypes.c_int),

@@ -1,0 +1,66 @@
+"""Launch-configuration autotuner for the fused step.
+
+The step is compiled in several launch configurations (block shape x register
+budget, SW_STEP_CONFIGS in csrc/sw_step.cuh).  Which one hides memory latency
+best depends on the storage type and the grid, so it is measured: each
+configuration steps the solver's current state into its spare lattice a few
+times (the state itself is not modified, and the spare lattice is overwritten
+by the next real step anyway), timed with CUDA events, and the fastest is
+installed for that storage type with sw_set_step_config.  Results are cached
+per (device name, dtype, grid) for the life of the process.
+"""
+import torch
+
+from . import _native as N
+from .fields import _stream
+
+_CACHE = {}
+
+
+def config_count():
+    return N.lib().sw_step_config_count()
+
+
+def time_configs(solver, repeats=8, warmup=2):
+    """Mean step time in ms of every configuration on the solver's grid."""
+    L = N.lib()
+    g = solver.grid
+    src, dst = solver.f[solver.cur], solver.f[1 - solver.cur]
+    stream = torch.cuda.current_stream()
+    res = {}
+    for cfg in range(config_count()):
+        def launch():
+            N.check(L.sw_step_cfg(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
+                                  solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge,
+                                  None, 0, None, cfg, _stream(stream)), "sw_step_cfg")
+        for _ in range(warmup):
+            launch()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(repeats):
+            launch()
+        e1.record()
+        torch.cuda.synchronize()
+        res[cfg] = e0.elapsed_time(e1) / repeats
+    return res
+
+
+def tune(solver, repeats=8, force=False):
+    """Pick and install the fastest configuration for the solver's storage type; returns (cfg, times)."""
+    g = solver.grid
+    key = (torch.cuda.get_device_name(solver.device), solver.dtype, g.nx, g.ny, g.nz)
+    if key in _CACHE and not force:
+        best, times = _CACHE[key]
+    else:
+        times = time_configs(solver, repeats=repeats)
+        best = min(times, key=times.get)
+        _CACHE[key] = (best, times)
+    N.check(N.lib().sw_set_step_config(solver.dtype, best), "sw_set_step_config")
+    return best, times
+
+
+def current(dtype):
+    return N.lib().sw_get_step_config(N.dtype_code(dtype))
+
+
+__all__ = ["tune", "time_configs", "config_count", "current"]

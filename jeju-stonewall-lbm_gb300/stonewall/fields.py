@@ -163,11 +163,17 @@ class Accum:
     def ptr(self):
         return _ptr(self.data)
 
-    def numpy(self, stream=None):
+    def numpy(self, stream=None, solid=None, n_acc=None):
+        """Sums in the reference layout.  With ``solid`` (bool (nx, ny, nz)) and ``n_acc`` the
+        non-fluid cells are set to n_acc * (1, 0, 0, 0), what k_macro + k_accum give them."""
         g = self.grid
         out = torch.empty((4, g.nx, g.ny, g.nz), dtype=torch.float64, device=self.data.device)
         N.check(N.lib().sw_unpack_acc(g.gp, self.ptr, _ptr(out), _stream(stream)), "sw_unpack_acc")
-        return out.cpu().numpy()
+        a = out.cpu().numpy()
+        if solid is not None:
+            a[0][solid] = float(n_acc)
+            a[1:, solid] = 0.0
+        return a
 
     def assign(self, acc_ref):
         """Load sums from the reference layout (4, nx, ny, nz) (resume, lbm3d.py:334)."""

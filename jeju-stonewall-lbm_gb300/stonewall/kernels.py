@@ -66,8 +66,12 @@ def k_init(f: Lattice, flag: Flags, uin, noise=0.02, seed=7, noise_kind="uniform
 
 
 def k_step(f_in: Lattice, f_out: Lattice, flag: Flags, uin, nx, ny, nz, nu0, cs, x_sponge, nu_sponge=0.05,
-           force: ForceSeries = None, t=0, stream=None):
-    """lbm3d.py:57-155: one fused timestep f_in -> f_out; force[t] receives the wall force."""
+           force: ForceSeries = None, t=0, stream=None, acc: Accum = None):
+    """lbm3d.py:57-155: one fused timestep f_in -> f_out; force[t] receives the wall force.
+
+    With ``acc`` the new state's (rho, u) of every fluid cell is also added to
+    the running sums (k_macro + k_accum of lbm3d.py:367-369 in the same pass).
+    """
     g = _same_grid(f_in, f_out, flag)
     if (int(nx), int(ny), int(nz)) != (g.nx, g.ny, g.nz):
         raise ValueError(f"extents {(nx, ny, nz)} do not match the fields' grid {g}")
@@ -78,9 +82,15 @@ def k_step(f_in: Lattice, f_out: Lattice, flag: Flags, uin, nx, ny, nz, nu0, cs,
         if force.nz != g.nz or not (0 <= int(t) < force.n_steps):
             raise ValueError(f"step {t} outside the force series ({force.n_steps} x {force.nz})")
         fptr = force.ptr
-    N.check(N.lib().sw_step(g.gp, f_in.dtype, f_in.ptr, f_out.ptr, flag.ptr, flag.tiles_ptr, _uin(uin).ptr,
-                            float(nu0), float(cs), int(x_sponge), float(nu_sponge), fptr, int(t),
-                            _stream(stream)), "sw_step")
+    if acc is None:
+        N.check(N.lib().sw_step(g.gp, f_in.dtype, f_in.ptr, f_out.ptr, flag.ptr, flag.tiles_ptr, _uin(uin).ptr,
+                                float(nu0), float(cs), int(x_sponge), float(nu_sponge), fptr, int(t),
+                                _stream(stream)), "sw_step")
+    else:
+        _same_grid(f_in, acc)
+        N.check(N.lib().sw_step_accum(g.gp, f_in.dtype, f_in.ptr, f_out.ptr, flag.ptr, flag.tiles_ptr,
+                                      _uin(uin).ptr, float(nu0), float(cs), int(x_sponge), float(nu_sponge), fptr,
+                                      int(t), acc.ptr, _stream(stream)), "sw_step_accum")
 
 
 def k_macro(f: Lattice, flag: Flags, u: Macro, stream=None):

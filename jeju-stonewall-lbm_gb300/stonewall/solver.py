@@ -84,17 +84,23 @@ class WallSolver:
         self.t, self.n_acc, self.cur = 0, 0, 0
         return self
 
+    def autotune(self, repeats=8):
+        """Time the step's launch configurations on this grid and install the fastest for this
+        storage type (stonewall.autotune); the state is not modified.  Returns (cfg, times)."""
+        from . import autotune
+        return autotune.tune(self, repeats=repeats)
+
     def init(self, noise=0.02, seed=7, noise_kind="uniform"):
         """k_init on the current lattice (lbm3d.py:340)."""
         K.k_init(self.state, self.flags, self.uin, noise, seed, noise_kind)
         return self
 
     # ------------------------------------------------------------ stepping
-    def _step(self, force_rows, t_index):
+    def _step(self, force_rows, t_index, accumulate=False):
         src, dst = self.f[self.cur], self.f[1 - self.cur]
         g = self.grid
         K.k_step(src, dst, self.flags, self.uin, g.nx, g.ny, g.nz, self.nu0, self.cs, self.x_sponge,
-                 self.nu_sponge, force_rows, t_index)
+                 self.nu_sponge, force_rows, t_index, acc=self.acc if accumulate else None)
         self.cur ^= 1
 
     def _accumulate_now(self, t):
@@ -104,12 +110,10 @@ class WallSolver:
         """One eager step (lbm3d.py:359-370)."""
         if self.t >= self.n_total:
             raise RuntimeError("the run is complete")
-        self._step(self.force, self.t)
+        acc = self._accumulate_now(self.t)
+        self._step(self.force, self.t, accumulate=acc)
         self.launches += 1
-        if self._accumulate_now(self.t):
-            K.k_macro_accum(self.state, self.flags, self.acc)
-            self.n_acc += 1
-            self.launches += 1
+        self.n_acc += int(acc)
         self.t += 1
 
     def _graph_for(self, key):
@@ -127,9 +131,7 @@ class WallSolver:
         with torch.cuda.graph(graph):
             ring.data.zero_()
             for j in range(n):
-                self._step(ring, j)
-                if phase is not None and (phase + j) % self.acc_every == 0:
-                    K.k_macro_accum(self.state, self.flags, self.acc)
+                self._step(ring, j, accumulate=phase is not None and (phase + j) % self.acc_every == 0)
         self.cur = saved_cur
         n_acc = 0 if phase is None else sum(1 for j in range(n) if (phase + j) % self.acc_every == 0)
         self._graphs[key] = (graph, n_acc)
@@ -150,7 +152,7 @@ class WallSolver:
                 self.cur ^= (c & 1)
                 self.t += c
                 self.n_acc += n_acc
-                self.launches += c + n_acc
+                self.launches += c
                 n -= c
             else:
                 self.step()
@@ -185,9 +187,13 @@ class WallSolver:
         """(n_total, nz, 2) float64."""
         return self.force.numpy()
 
+    def sums(self):
+        """Running sums of (rho, u), reference layout, solids at n_acc * (1, 0, 0, 0) (lbm3d.py:303)."""
+        return self.acc.numpy(solid=self.flags.host != 0, n_acc=self.n_acc)
+
     def mean_field(self):
         """Time-mean (rho, u) over the accumulated states, float64 (lbm3d.py:402)."""
-        return self.acc.numpy() / max(self.n_acc, 1)
+        return self.sums() / max(self.n_acc, 1)
 
     # ------------------------------------------------------------ checkpoints
     def save_checkpoint(self, path, sig, extra=None):
@@ -198,7 +204,7 @@ class WallSolver:
         ref_dtype = np.float64 if self.dtype == 1 else np.float32
         np.save(os.path.join(tmp, "f.npy"), self.state.numpy(ref_dtype))
         np.save(os.path.join(tmp, "force.npy"), self.force.numpy())
-        np.save(os.path.join(tmp, "uacc.npy"), self.acc.numpy())
+        np.save(os.path.join(tmp, "uacc.npy"), self.sums())
         g = self.grid
         extra = extra or {}
         np.save(os.path.join(tmp, "snaps_xz.npy"), extra.get("snaps_xz", np.zeros((0, 3, g.nx, g.nz), np.float16)))

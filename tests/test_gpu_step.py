@@ -68,6 +68,31 @@ def test_macro_and_accum_bit_exact(cuda):
     np.testing.assert_array_equal(acc2.numpy(), acc.numpy())
 
 
+def test_step_accum_matches_macro_accum(cuda):
+    """sw_step_accum adds the new state's (rho, u) to the sums in the same pass (fluid cells)."""
+    from stonewall.fields import Accum, Flags, ForceSeries, Grid, Lattice
+    from stonewall.kernels import DeviceVector, k_macro_accum, k_step
+    d = golden("step_rand")
+    nu0, cs, xs, nus, noise, seed, n = _params(d)
+    nx, ny, nz = d["flag"].shape
+    grid = Grid(nx, ny, nz)
+    flags = Flags(grid, d["flag"])
+    uv = DeviceVector(d["uin"])
+    src = Lattice(grid).assign(d["f_init"])
+    a, b = Lattice(grid).zero_(), Lattice(grid).zero_()
+    fused, sep = Accum(grid), Accum(grid)
+    fa, fb = ForceSeries(1, nz), ForceSeries(1, nz)
+    for _ in range(2):
+        k_step(src, a, flags, uv, nx, ny, nz, nu0, cs, xs, nus, fa, 0, acc=fused)
+        k_step(src, b, flags, uv, nx, ny, nz, nu0, cs, xs, nus, fb, 0)
+        k_macro_accum(b, flags, sep)
+    assert_fields_close(a.numpy(), b.numpy(), d["flag"], 1e-6)
+    assert_force_close(fa.numpy(), fb.numpy(), 1e-6)
+    solid = d["flag"] != 0
+    got, want = fused.numpy(solid=solid, n_acc=2), sep.numpy()
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-7)
+
+
 def test_launch_mirror_matches_direct(cuda):
     """launch(k_step, dim, [reference input list]) runs the same kernel as k_step()."""
     from stonewall import kernels as K
@@ -130,3 +155,34 @@ def test_force_deterministic(cuda):
     a = gpu_run(d["flag"], d["uin"], d["f_init"], nu0, cs, xs, nus, n)[2]
     b = gpu_run(d["flag"], d["uin"], d["f_init"], nu0, cs, xs, nus, n)[2]
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16", "bf16", "f64"])
+def test_every_launch_configuration_computes_the_same_step(dtype, cuda):
+    """The compiled launch configurations differ in block shape and register budget only."""
+    import ctypes
+    import torch
+    from stonewall import _native as N
+    from stonewall.fields import Flags, ForceSeries, Grid, Lattice
+    from stonewall.kernels import DeviceVector
+    nx, ny, nz = 70, 13, 11
+    flag = make_mask(nx, ny, nz, 7)
+    uin = inlet(nz, 3)
+    from oracle import oracle
+    f0 = oracle.init(flag, uin, noise=0.05, seed=7)
+    grid = Grid(nx, ny, nz)
+    flags = Flags(grid, flag)
+    uv = DeviceVector(uin)
+    src = Lattice(grid, dtype).assign(f0)
+    L = N.lib()
+    outs = []
+    for cfg in range(L.sw_step_config_count()):
+        dst = Lattice(grid, dtype).zero_()
+        force = ForceSeries(1, nz)
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        N.check(L.sw_step_cfg(grid.gp, src.dtype, src.ptr, dst.ptr, flags.ptr, flags.tiles_ptr, uv.ptr, 2e-3, 0.1,
+                              nx - 10, 0.05, force.ptr, 0, None, cfg, st), "sw_step_cfg")
+        outs.append((dst.numpy(np.float64), force.numpy()))
+    for f, fo in outs[1:]:
+        np.testing.assert_array_equal(f, outs[0][0])
+        np.testing.assert_array_equal(fo, outs[0][1])
