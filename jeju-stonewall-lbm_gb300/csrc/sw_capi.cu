@@ -138,6 +138,7 @@ int step_impl(const sw_geom *g, int dtype, const void *f_in, void *f_out, const 
               int64_t t, double *acc, int cfg, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f_in || !f_out || !flag || !tiles || !uin) return SW_ERR_BAD_ARG;
   if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
+  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
   if (f_in == f_out || !aligned16(f_in) || !aligned16(f_out) || t < 0) return SW_ERR_BAD_ARG;
   sw::StepParams p;
   p.fin = f_in;
@@ -190,6 +191,7 @@ int sw_step_config_count(void) { return sw::kStepConfigs; }
 
 int sw_set_step_config(int dtype, int cfg) {
   if (!dtype_ok(dtype) || cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
+  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
   g_step_cfg[dtype] = cfg;
   return SW_OK;
 }

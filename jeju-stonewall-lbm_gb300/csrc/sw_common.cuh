@@ -96,6 +96,8 @@ template <> struct Store<SW_F16_SHIFT> {
   template <int I> static __device__ __forceinline__ T enc(R v) { return __float2half_rn(v - W<float>(I)); }
   template <int I> static __device__ __forceinline__ R ld(const T *p) { return __half2float(__ldg(p)); }
   template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, __float2half_rn(v)); }
+  static __device__ __forceinline__ T from_shifted(R g) { return __float2half_rn(g); }
+  static __device__ __forceinline__ R to_shifted(T v) { return __half2float(v); }
 };
 template <> struct Store<SW_BF16_SHIFT> {
   using T = __nv_bfloat16;
@@ -105,6 +107,8 @@ template <> struct Store<SW_BF16_SHIFT> {
   template <int I> static __device__ __forceinline__ T enc(R v) { return __float2bfloat16_rn(v - W<float>(I)); }
   template <int I> static __device__ __forceinline__ R ld(const T *p) { return __bfloat162float(__ldg(p)); }
   template <int I> static __device__ __forceinline__ void st(T *p, R v) { __stcs(p, __float2bfloat16_rn(v)); }
+  static __device__ __forceinline__ T from_shifted(R g) { return __float2bfloat16_rn(g); }
+  static __device__ __forceinline__ R to_shifted(T v) { return __bfloat162float(v); }
 };
 
 // lbm3d.py:33-36, same evaluation order.

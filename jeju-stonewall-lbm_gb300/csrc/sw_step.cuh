@@ -44,10 +44,37 @@ struct StepParams {
   long long *force;  // force row of this step: [nz][2], or nullptr
   double *acc;       // float64 running sums [4][plane] (accumulation steps only)
   int cfg;           // launch configuration (SW_STEP_CONFIGS)
+  // per-population plane bases (fin + i * plane etc.), uniform across the grid,
+  // so that every load and store needs only a 32-bit offset within a plane
+  const void *fin_pop[Q];
+  void *fout_pop[Q];
+  double *acc_pop[4];
 };
 
-__device__ __forceinline__ float rcp(float v) { return __frcp_rn(v); }
+// Fills the per-population bases from fin / fout / acc (host side).
+inline void set_plane_bases(StepParams &p, size_t elem_bytes) {
+  const size_t pb = (size_t)p.g.plane * elem_bytes;
+  for (int i = 0; i < Q; ++i) {
+    p.fin_pop[i] = static_cast<const char *>(p.fin) + i * pb;
+    p.fout_pop[i] = static_cast<char *>(p.fout) + i * pb;
+  }
+  for (int k = 0; k < 4; ++k) p.acc_pop[k] = p.acc ? p.acc + (size_t)k * p.g.plane : nullptr;
+}
+
+// float: the hardware approximations (relative error about 2^-23, far below the
+// 1e-5 parity bar); double: IEEE division and square root.
+__device__ __forceinline__ float rcp(float v) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
 __device__ __forceinline__ double rcp(double v) { return 1.0 / v; }
+__device__ __forceinline__ float fsqrt(float v) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+__device__ __forceinline__ double fsqrt(double v) { return sqrt(v); }
 
 // Regularized-BGK collision of one cell from its 19 pulled populations.
 // Calls put(Int<i>, value) for every population and returns rho and u.
@@ -94,8 +121,8 @@ __device__ __forceinline__ void collide(const R (&f)[Q], int x, R nu0, R cs2_18r
     nu = nu0 + nu_sponge * sp * sp;
   }
   const R tau0 = R(3.0) * nu + R(0.5);
-  const R qn = sqrt(nxx * nxx + nyy * nyy + nzz * nzz + R(2.0) * (nxy * nxy + nxz * nxz + nyz * nyz));
-  const R tau = R(0.5) * (tau0 + sqrt(tau0 * tau0 + cs2_18r2 * qn * inv));
+  const R qn = fsqrt(nxx * nxx + nyy * nyy + nzz * nzz + R(2.0) * (nxy * nxy + nxz * nxz + nyz * nyz));
+  const R tau = R(0.5) * (tau0 + fsqrt(tau0 * tau0 + cs2_18r2 * qn * inv));
   const R keep = R(1.0) - rcp(tau);
   // B = rho u u + keep Pi_neq and the pair terms of Q_i : B
   const R bxx = mx * ux + keep * nxx, byy = my * uy + keep * nyy, bzz = mz * uz + keep * nzz;
@@ -138,23 +165,23 @@ template <int WY_, int MINB_> struct StepCfg {
   static constexpr int THREADS = 32 * WY_;
 };
 #define SW_STEP_CONFIGS(X) X(0, 8, 4) X(1, 8, 5) X(2, 4, 8) X(3, 4, 12)
-constexpr int kStepConfigs = 4;
+// two cells per thread (16-bit storage only), see k_step_pair
+#define SW_PAIR_CONFIGS(X) X(4, 4, 8) X(5, 4, 10) X(6, 8, 4) X(7, 8, 5)
+constexpr int kStepConfigs = 8;
 
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
-// tests (segments next to stones, the ground or a fluid cell at z = 0).  Idx is
-// the type of element offsets into a lattice: int when 19 planes fit in 2^31
-// elements (every grid up to 113 M cells), long long otherwise.
-template <int DT, bool CHECK, bool ACC, typename Idx>
+// tests (segments next to stones, the ground or a fluid cell at z = 0).
+// Offsets within a population plane are 32-bit (grids below 2^31 cells).
+template <int DT, bool CHECK, bool ACC>
 __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int z, typename Store<DT>::R &fxw,
                                           typename Store<DT>::R &fzw, int &hit) {
   using S = Store<DT>;
   using T = typename S::T;
   using R = typename S::R;
   const Geom &g = p.g;
-  const Idx plane = (Idx)g.plane;
   const int c = (z * g.ny + y) * g.pitch + x;
-  const T *__restrict__ fin = static_cast<const T *>(p.fin);
-  T *__restrict__ fout = static_cast<T *>(p.fout);
+  auto in = [&](int pop) { return static_cast<const T *>(p.fin_pop[pop]); };
+  auto out = [&](int pop) { return static_cast<T *>(p.fout_pop[pop]); };
   if (CHECK && p.flag[c] != 0) return;                          // lbm3d.py:65-66
   if (x == 0) {                                                 // inlet, lbm3d.py:67-71
     const R u0 = (R)__ldg(p.uin + z);
@@ -166,11 +193,11 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
       if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
       cu = R(3.0) * cu;
       const R v = W<R>(i) * R(1.0) * (R(1.0) + cu + R(0.5) * cu * cu - R(1.5) * usq);
-      S::template st<i>(fout + ((Idx)i * plane + c), S::kShift ? v - W<R>(i) : v);
+      S::template st<i>(out(i) + c, S::kShift ? v - W<R>(i) : v);
     });
     if (ACC) {
-      atomicAdd(p.acc + c, 1.0);
-      atomicAdd(p.acc + ((Idx)plane + c), (double)u0);
+      atomicAdd(p.acc_pop[0] + c, 1.0);
+      atomicAdd(p.acc_pop[1] + c, (double)u0);
     }
     return;
   }
@@ -197,7 +224,7 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
       const uint8_t fs = (ez == 1 && z == 0) ? (uint8_t)SW_GROUND : __ldg(p.flag + src);
       if (fs != 0) {                                            // lbm3d.py:89-95
         pull = false;
-        const R val = S::template ld<OPP(i)>(fin + ((Idx)OPP(i) * plane + c));
+        const R val = S::template ld<OPP(i)>(in(OPP(i)) + c);
         if (fs == SW_WALL) {
           const R fr = S::kShift ? val : val - W<R>(i);   // f - w, the rho = 1 background removed
           if constexpr (ex != 0) fxw = fxw - R(2.0) * fr * R(ex);
@@ -209,10 +236,10 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
     }
     if (pull) {                                                 // lbm3d.py:97
       if constexpr (ez == -1) {
-        if (top) fl[i] = S::template ld<MIRZ(i)>(fin + ((Idx)MIRZ(i) * plane + src));
-        else fl[i] = S::template ld<i>(fin + ((Idx)i * plane + src));
+        if (top) fl[i] = S::template ld<MIRZ(i)>(in(MIRZ(i)) + src);
+        else fl[i] = S::template ld<i>(in(i) + src);
       } else {
-        fl[i] = S::template ld<i>(fin + ((Idx)i * plane + src));
+        fl[i] = S::template ld<i>(in(i) + src);
       }
     }
   });
@@ -221,20 +248,38 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
   collide<R, S::kShift>(fl, x, (R)p.nu0, R(18.0) * sqrt(R(2.0)) * cs * cs, p.x_sponge, (R)p.sponge_scale,
                         (R)p.nu_sponge, rho, ux, uy, uz, [&](auto I, R v) {
                           constexpr int i = decltype(I)::value;
-                          S::template st<i>(fout + ((Idx)i * plane + c), v);
+                          S::template st<i>(out(i) + c, v);
                         });
   if (ACC) {  // each cell is owned by one thread: reductions without a return value (no read stall)
-    double *a = p.acc;
-    atomicAdd(a + c, (double)rho);
-    atomicAdd(a + ((Idx)plane + c), (double)ux);
-    atomicAdd(a + ((Idx)2 * plane + c), (double)uy);
-    atomicAdd(a + ((Idx)3 * plane + c), (double)uz);
+    atomicAdd(p.acc_pop[0] + c, (double)rho);
+    atomicAdd(p.acc_pop[1] + c, (double)ux);
+    atomicAdd(p.acc_pop[2] + c, (double)uy);
+    atomicAdd(p.acc_pop[3] + c, (double)uz);
+  }
+}
+
+// Adds the warp's wall force (lbm3d.py:99-101): float64 xor-butterfly sum, then
+// one 2^-40 fixed-point integer atomic per component.
+template <typename R>
+__device__ __forceinline__ void warp_force_add(const StepParams &p, int z, int lane, R fxw, R fzw, int hit) {
+  double dx = (double)fxw, dz = (double)fzw;
+  const unsigned any = __ballot_sync(0xffffffffu, hit);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dx += __shfl_xor_sync(0xffffffffu, dx, o);
+    dz += __shfl_xor_sync(0xffffffffu, dz, o);
+  }
+  if (lane == 0 && any) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(p.force + 2 * z),
+              (unsigned long long)__double2ll_rn(dx * FORCE_SCALE));
+    atomicAdd(reinterpret_cast<unsigned long long *>(p.force + 2 * z + 1),
+              (unsigned long long)__double2ll_rn(dz * FORCE_SCALE));
   }
 }
 
 // Grid: (pitch / 32, ceil(ny / WY), nz); warp (threadIdx.y) = one row segment.
-template <int DT, bool ACC, typename Idx, typename Cfg>
-__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(StepParams p) {
+template <int DT, bool ACC, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(const __grid_constant__ StepParams p) {
   using R = typename Store<DT>::R;
   const Geom &g = p.g;
   const int y = blockIdx.y * Cfg::WY + threadIdx.y;
@@ -248,51 +293,199 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(StepParam
   R fxw = R(0.0), fzw = R(0.0);
   int hit = 0;
   if (!(kind & TILE_CHECK)) {
-    if (x < g.nx) step_cell<DT, false, ACC, Idx>(p, x, y, z, fxw, fzw, hit);
+    if (x < g.nx) step_cell<DT, false, ACC>(p, x, y, z, fxw, fzw, hit);
     return;
   }
-  if (x < g.nx) step_cell<DT, true, ACC, Idx>(p, x, y, z, fxw, fzw, hit);
-  if ((kind & TILE_FORCE) && p.force != nullptr) {              // lbm3d.py:99-101
-    double dx = (double)fxw, dz = (double)fzw;
-    const unsigned any = __ballot_sync(0xffffffffu, hit);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      dx += __shfl_xor_sync(0xffffffffu, dx, o);
-      dz += __shfl_xor_sync(0xffffffffu, dz, o);
+  if (x < g.nx) step_cell<DT, true, ACC>(p, x, y, z, fxw, fzw, hit);
+  if ((kind & TILE_FORCE) && p.force != nullptr) warp_force_add<R>(p, z, lane, fxw, fzw, hit);
+}
+
+// ---------------------------------------------------------------- two cells per thread, 16-bit storage
+// One 32-bit load carries the populations of cells x0 and x0 + 1 (x0 even); a
+// warp covers 64 cells of a row.  Pulls along x take the neighbouring cell's
+// half from the adjacent lane (warp shuffle); the first and last lane load the
+// cell just outside the warp's 64 directly.  Outputs are packed two per 32-bit
+// store.  Warps whose segments need flag tests run the per-cell path for both
+// of their cells.
+template <int DT> struct Pack16;
+template <> struct Pack16<SW_F16_SHIFT> {
+  static __device__ __forceinline__ float lo(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v & 0xffffu))); }
+  static __device__ __forceinline__ float hi(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v >> 16))); }
+  static __device__ __forceinline__ float one(const __half *q) { return __half2float(__ldg(q)); }
+  static __device__ __forceinline__ uint32_t pack(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
+  }
+};
+template <> struct Pack16<SW_BF16_SHIFT> {
+  static __device__ __forceinline__ float lo(uint32_t v) { return __uint_as_float(v << 16); }
+  static __device__ __forceinline__ float hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
+  static __device__ __forceinline__ float one(const __nv_bfloat16 *q) { return __bfloat162float(__ldg(q)); }
+  static __device__ __forceinline__ uint32_t pack(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
+  }
+};
+
+template <int DT, bool ACC>
+__device__ __forceinline__ void step_pair_fast(const StepParams &p, int x0, int y, int z, int lane) {
+  using S = Store<DT>;
+  using T = typename S::T;
+  using PK = Pack16<DT>;
+  const Geom &g = p.g;
+  const bool live = x0 < g.nx;        // cell x0 exists; the 32-bit pair lies inside the row
+  const bool has_b = x0 + 1 < g.nx;   // cell x0 + 1 exists
+  const bool has_r = x0 + 2 < g.nx;   // cell x0 + 2 exists (else the outlet copies x0 + 1)
+  const int c = (z * g.ny + y) * g.pitch + x0;
+  auto in = [&](int pop) { return static_cast<const T *>(p.fin_pop[pop]); };
+  auto out = [&](int pop) { return static_cast<T *>(p.fout_pop[pop]); };
+  const int row = g.pitch, lev = g.ny * g.pitch;
+  const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
+  const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
+  const bool top = (z == g.nz - 1);
+  const int off_zm = -lev;
+  const int off_zp = top ? 0 : lev;
+  // phase 1: every load in flight before the first shuffle consumes one
+  uint32_t P[Q];
+  float edge[Q];                                        // lane 0: cell x0 - 1, lane 31: cell x0 + 2
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
+    const int rowoff = (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) + (ez == 1 ? off_zm : ez == -1 ? off_zp : 0);
+    const T *base = ((ez == -1 && top) ? in(MIRZ(i)) : in(i)) + (c + rowoff);   // source row, column x0
+    P[i] = live ? __ldg(reinterpret_cast<const unsigned int *>(base)) : 0u;
+    if constexpr (ex == 1) edge[i] = (lane == 0 && live && x0 > 0) ? PK::one(base - 1) : 0.0f;
+    if constexpr (ex == -1) edge[i] = (lane == 31 && live && has_r) ? PK::one(base + 2) : 0.0f;
+  });
+  // phase 2: pulls along x from the neighbouring lanes (outlet copies column x)
+  float a[Q], b[Q];
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = CX(i);
+    if constexpr (ex == 0) {
+      a[i] = PK::lo(P[i]);
+      b[i] = PK::hi(P[i]);
+    } else if constexpr (ex == 1) {                     // sources x0 - 1, x0
+      const uint32_t prev = __shfl_up_sync(0xffffffffu, P[i], 1);
+      a[i] = lane == 0 ? edge[i] : PK::hi(prev);
+      b[i] = PK::lo(P[i]);
+    } else {                                            // sources x0 + 1, x0 + 2
+      const uint32_t next = __shfl_down_sync(0xffffffffu, P[i], 1);
+      const float right = lane == 31 ? edge[i] : PK::lo(next);
+      a[i] = has_b ? PK::hi(P[i]) : PK::lo(P[i]);
+      b[i] = has_r ? right : PK::hi(P[i]);
     }
-    if (lane == 0 && any) {
-      atomicAdd(reinterpret_cast<unsigned long long *>(p.force + 2 * z),
-                (unsigned long long)__double2ll_rn(dx * FORCE_SCALE));
-      atomicAdd(reinterpret_cast<unsigned long long *>(p.force + 2 * z + 1),
-                (unsigned long long)__double2ll_rn(dz * FORCE_SCALE));
+  });
+  if (!live) return;
+  const float cs = (float)p.cs;
+  const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
+  T oa[Q];
+  float ra, uxa, uya, uza;
+  collide<float, true>(a, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, ra, uxa,
+                       uya, uza, [&](auto I, float v) {
+                         constexpr int i = decltype(I)::value;
+                         oa[i] = S::from_shifted(v);
+                       });
+  if (x0 == 0) {                                        // inlet cell, lbm3d.py:67-71
+    const float u0 = __ldg(p.uin + z);
+    static_for<0, Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      constexpr int ex = CX(i);
+      float cu = 0.0f;
+      if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
+      cu = 3.0f * cu;
+      oa[i] = S::from_shifted(W<float>(i) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * (u0 * u0)) - W<float>(i));
+    });
+    ra = 1.0f; uxa = u0; uya = 0.0f; uza = 0.0f;
+  }
+  float rb, uxb, uyb, uzb;
+  collide<float, true>(b, x0 + 1, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rb, uxb,
+                       uyb, uzb, [&](auto I, float v) {
+                         constexpr int i = decltype(I)::value;
+                         const float va = S::to_shifted(oa[i]);
+                         if (has_b) __stcs(reinterpret_cast<unsigned int *>(out(i) + c), PK::pack(va, v));
+                         else __stcs(out(i) + c, oa[i]);
+                       });
+  if (ACC) {
+    atomicAdd(p.acc_pop[0] + c, (double)ra);
+    atomicAdd(p.acc_pop[1] + c, (double)uxa);
+    atomicAdd(p.acc_pop[2] + c, (double)uya);
+    atomicAdd(p.acc_pop[3] + c, (double)uza);
+    if (has_b) {
+      atomicAdd(p.acc_pop[0] + c + 1, (double)rb);
+      atomicAdd(p.acc_pop[1] + c + 1, (double)uxb);
+      atomicAdd(p.acc_pop[2] + c + 1, (double)uyb);
+      atomicAdd(p.acc_pop[3] + c + 1, (double)uzb);
     }
   }
 }
 
-template <int DT, bool ACC, typename Idx, typename Cfg>
+// Grid: (ceil(pitch / 64), ceil(ny / WY), nz); warp = two adjacent row segments.
+template <int DT, bool ACC, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pair(const __grid_constant__ StepParams p) {
+  const Geom &g = p.g;
+  const int y = blockIdx.y * Cfg::WY + threadIdx.y;
+  if (y >= g.ny) return;
+  const int z = blockIdx.z;
+  const int lane = threadIdx.x;
+  const int sa = 2 * blockIdx.x;
+  const bool has_tb = sa + 1 < g.nseg_x;
+  const int seg = (z * g.ny + y) * g.nseg_x + sa;
+  const uint8_t ka = __ldg(p.tiles + seg);
+  const uint8_t kb = has_tb ? __ldg(p.tiles + seg + 1) : (uint8_t)TILE_ALL_SOLID;
+  if ((ka & kb & TILE_ALL_SOLID)) return;
+  const int x0 = 2 * SEG * blockIdx.x + 2 * lane;
+  if (!((ka | kb) & TILE_CHECK)) {
+    step_pair_fast<DT, ACC>(p, x0, y, z, lane);
+    return;
+  }
+  float fxw = 0.0f, fzw = 0.0f;
+  int hit = 0;
+  if (x0 < g.nx) step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
+  if (x0 + 1 < g.nx) step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
+  if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+}
+
+template <int DT, bool ACC, typename Cfg>
 cudaError_t launch_cfg(const StepParams &p, cudaStream_t s) {
   const dim3 grid((unsigned)p.g.nseg_x, (unsigned)((p.g.ny + Cfg::WY - 1) / Cfg::WY), (unsigned)p.g.nz);
   const dim3 block(32, Cfg::WY);
-  k_step_pull<DT, ACC, Idx, Cfg><<<grid, block, 0, s>>>(p);
+  k_step_pull<DT, ACC, Cfg><<<grid, block, 0, s>>>(p);
   return cudaGetLastError();
 }
 
-// Narrow grids (19 planes < 2^31 elements) run the chosen configuration;
-// wider ones run configuration 0 with 64-bit offsets.
+template <int DT, bool ACC, typename Cfg>
+cudaError_t launch_pair(const StepParams &p, cudaStream_t s) {
+  const dim3 grid((unsigned)((p.g.nseg_x + 1) / 2), (unsigned)((p.g.ny + Cfg::WY - 1) / Cfg::WY), (unsigned)p.g.nz);
+  const dim3 block(32, Cfg::WY);
+  k_step_pair<DT, ACC, Cfg><<<grid, block, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+constexpr bool is16(int dt) { return dt == SW_F16_SHIFT || dt == SW_BF16_SHIFT; }
+
+// Whether configuration cfg exists for storage type dt.
+inline bool step_config_valid(int dt, int cfg) { return (cfg >= 0 && cfg < 4) || (cfg >= 4 && cfg < 8 && is16(dt)); }
+
 template <int DT>
-cudaError_t launch_step(const StepParams &p, cudaStream_t s) {
-  const bool narrow = (long long)Q * p.g.plane < (1ll << 31);
-  if (p.g.nz > 65535) return cudaErrorInvalidValue;
-  if (!narrow) {
-    using C0 = StepCfg<8, 4>;
-    return p.acc ? launch_cfg<DT, true, long long, C0>(p, s) : launch_cfg<DT, false, long long, C0>(p, s);
-  }
+cudaError_t launch_step(const StepParams &p_in, cudaStream_t s) {
+  if (p_in.g.nz > 65535 || (p_in.g.ny + 3) / 4 > 65535) return cudaErrorInvalidValue;
+  StepParams p = p_in;
+  set_plane_bases(p, sizeof(typename Store<DT>::T));
   switch (p.cfg) {
 #define SW_CASE(ID, WY, MINB)                                                                      \
   case ID:                                                                                         \
-    return p.acc ? launch_cfg<DT, true, int, StepCfg<WY, MINB>>(p, s)                             \
-                 : launch_cfg<DT, false, int, StepCfg<WY, MINB>>(p, s);
+    return p.acc ? launch_cfg<DT, true, StepCfg<WY, MINB>>(p, s) : launch_cfg<DT, false, StepCfg<WY, MINB>>(p, s);
     SW_STEP_CONFIGS(SW_CASE)
+#undef SW_CASE
+#define SW_CASE(ID, WY, MINB)                                                                      \
+  case ID:                                                                                         \
+    if constexpr (is16(DT))                                                                        \
+      return p.acc ? launch_pair<DT, true, StepCfg<WY, MINB>>(p, s)                               \
+                   : launch_pair<DT, false, StepCfg<WY, MINB>>(p, s);                             \
+    else                                                                                           \
+      return cudaErrorNotSupported;
+    SW_PAIR_CONFIGS(SW_CASE)
 #undef SW_CASE
     default:
       return cudaErrorInvalidValue;

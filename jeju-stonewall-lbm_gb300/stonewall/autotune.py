@@ -29,6 +29,11 @@ def time_configs(solver, repeats=8, warmup=2):
     stream = torch.cuda.current_stream()
     res = {}
     for cfg in range(config_count()):
+        if L.sw_step_cfg(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
+                         solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge, None, 0, None,
+                         cfg, _stream(stream)) == N.SW_ERR_UNSUPPORTED:
+            continue                                  # not compiled for this storage type
+
         def launch():
             N.check(L.sw_step_cfg(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
                                   solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge,

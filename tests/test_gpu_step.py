@@ -15,6 +15,7 @@ pytestmark = pytest.mark.gpu
 
 RTOL_F32 = 1e-5
 RTOL_F64 = 1e-12
+W_REF = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
 
 
 def _params(d):
@@ -159,7 +160,11 @@ def test_force_deterministic(cuda):
 
 @pytest.mark.parametrize("dtype", ["f32", "f16", "bf16", "f64"])
 def test_every_launch_configuration_computes_the_same_step(dtype, cuda):
-    """The compiled launch configurations differ in block shape and register budget only."""
+    """The compiled launch configurations differ in block shape and register budget only.
+
+    Configurations 4-7 (16-bit storage) take two cells per thread; they run the same
+    collision but may round an intermediate differently, so they are held to a few
+    units of the storage format's last place instead of bit equality."""
     import ctypes
     import torch
     from stonewall import _native as N
@@ -175,14 +180,25 @@ def test_every_launch_configuration_computes_the_same_step(dtype, cuda):
     uv = DeviceVector(uin)
     src = Lattice(grid, dtype).assign(f0)
     L = N.lib()
-    outs = []
+    outs = {}
     for cfg in range(L.sw_step_config_count()):
         dst = Lattice(grid, dtype).zero_()
         force = ForceSeries(1, nz)
         st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-        N.check(L.sw_step_cfg(grid.gp, src.dtype, src.ptr, dst.ptr, flags.ptr, flags.tiles_ptr, uv.ptr, 2e-3, 0.1,
-                              nx - 10, 0.05, force.ptr, 0, None, cfg, st), "sw_step_cfg")
-        outs.append((dst.numpy(np.float64), force.numpy()))
-    for f, fo in outs[1:]:
-        np.testing.assert_array_equal(f, outs[0][0])
-        np.testing.assert_array_equal(fo, outs[0][1])
+        rc = L.sw_step_cfg(grid.gp, src.dtype, src.ptr, dst.ptr, flags.ptr, flags.tiles_ptr, uv.ptr, 2e-3, 0.1,
+                           nx - 10, 0.05, force.ptr, 0, None, cfg, st)
+        if rc == N.SW_ERR_UNSUPPORTED:
+            assert dtype in ("f32", "f64") and cfg >= 4
+            continue
+        N.check(rc, "sw_step_cfg")
+        outs[cfg] = (dst.numpy(np.float64), force.numpy())
+    assert len(outs) == (8 if dtype in ("f16", "bf16") else 4)
+    for cfg, (f, fo) in outs.items():
+        ref = outs[0] if cfg < 4 else outs[4]
+        np.testing.assert_array_equal(f, ref[0])
+        np.testing.assert_array_equal(fo, ref[1])
+    if 4 in outs:
+        ulp = 2.0 ** -11 if dtype == "f16" else 2.0 ** -8     # relative precision of the stored deviation
+        dev = np.abs(outs[0][0] - W_REF[:, None, None, None])
+        np.testing.assert_allclose(outs[4][0], outs[0][0], rtol=0, atol=float(4 * ulp * dev.max()))
+        np.testing.assert_allclose(outs[4][1], outs[0][1], rtol=1e-3, atol=1e-6)
