@@ -149,6 +149,52 @@ int sw_accum(const sw_geom *g, const float *u, double *acc, sw_stream s);
 int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, double *acc,
                    sw_stream s);
 
+/* ---------------------------------------------------------------- batches
+ * Many independent lattices (walls of different sizes) advanced by one
+ * persistent launch per step.  No reference counterpart: the reference runs
+ * one wall per process (run_all.sh:11-17 runs the cases one after another).
+ * The caller keeps a table of entries in device memory; sw_batch_prepare
+ * (host only) validates it and fills the work-item fields and the header.
+ * The kernel reads table and header at run time, so a captured CUDA graph of
+ * sw_batch_step launches serves any composition that fits: rewrite t0 /
+ * steps_left / cur0 (and entries and header) between replays. */
+typedef struct sw_batch_entry {
+  sw_geom geom;          /* extents and pitch (sw_geom_make) */
+  int64_t item0;         /* first work item of this lattice   (set by sw_batch_prepare) */
+  int64_t items;         /* work items per step of this lattice (set by sw_batch_prepare) */
+  void *f[2];            /* the two population buffers (device layout, the batch's storage type) */
+  const uint8_t *flag;   /* device layout */
+  const uint8_t *tiles;  /* sw_build_tiles */
+  const float *uin;      /* [nz] */
+  int64_t *force;        /* [n_total][nz][2] fixed point, row t0 + k is written; or NULL */
+  double *acc;           /* [4][nz][ny][pitch] float64 sums, or NULL */
+  double nu0, cs, nu_sponge;
+  int32_t x_sponge;
+  int32_t n_spin;        /* accumulate on steps t >= n_spin with (t - n_spin) % acc_every == 0 */
+  int32_t acc_every;
+  int32_t cur0;          /* buffer (0 or 1) holding the state at k = 0 */
+  int64_t t0;            /* step index of launch k = 0 */
+  int64_t steps_left;    /* launches with k >= steps_left leave the lattice untouched */
+} sw_batch_entry;
+
+typedef struct sw_batch_header {
+  int32_t n;             /* entries in the table */
+  int32_t reserved;
+  int64_t total_items;   /* sum of items (set by sw_batch_prepare) */
+} sw_batch_header;
+
+/* Host only: check entries[0..n) for storage type dtype and configuration cfg
+ * and fill item0 / items and *hdr. */
+int sw_batch_prepare(sw_batch_entry *entries, int32_t n, int dtype, int cfg, sw_batch_header *hdr);
+/* Queries the device once for the persistent grid of (dtype, cfg); sw_batch_step
+ * does the same on first use, so call this first when the launches are to be
+ * captured in a CUDA graph. */
+int sw_batch_setup(int dtype, int cfg);
+/* Launch k of a batch step: every entry with k < steps_left advances from
+ * buffer (cur0 + k) & 1 to the other one, as sw_step / sw_step_accum would. */
+int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_dev, int dtype, int cfg, int32_t k,
+                  sw_stream s);
+
 /* force rows (fixed point) -> double, n values. */
 int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s);
 

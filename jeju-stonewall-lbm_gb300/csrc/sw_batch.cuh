@@ -1,0 +1,182 @@
+// sw_batch.cuh -- many lattices, one persistent launch per step.
+//
+// The lattices of a batch are described by a table in device memory
+// (sw_batch_entry, include/stonewall.h): geometry, the two ping-pong buffers,
+// flags, segment classes, inlet, force series, float64 sums, physics, and the
+// per-lattice step counter t0 and remaining steps.  A step of the batch is one
+// launch of k_step_batch with a grid of (SMs x resident blocks) that walks all
+// work items of all lattices (an item = one block's rows of one lattice), so
+// lattices of any size share the GPU in one launch.  The kernel reads the
+// table at run time: a CUDA graph of K launches (k = 0..K-1) captured once
+// serves any batch composition -- the host rewrites the table (and the header
+// with the count) between replays to admit, advance and retire lattices.
+//
+// Each lattice's cells are computed by the same cell code as the single-lattice
+// step; force rows use integer atomics and the sums are owned per cell, so a
+// lattice's results do not depend on what else is in the batch.
+#pragma once
+#include "sw_step.cuh"
+
+namespace sw {
+
+// Cell-code context of one batched lattice: population planes at pop * plane.
+struct BatchCtx {
+  Geom g;
+  const void *fin;
+  void *fout;
+  const uint8_t *flag;
+  const uint8_t *tiles;
+  const float *uin;
+  double nu0, cs, nu_sponge, sponge_scale;
+  int x_sponge;
+  long long *force;
+  double *acc;
+  template <typename T> __device__ __forceinline__ const T *in(int pop) const {
+    return static_cast<const T *>(fin) + (size_t)pop * (size_t)g.plane;
+  }
+  template <typename T> __device__ __forceinline__ T *out(int pop) const {
+    return static_cast<T *>(fout) + (size_t)pop * (size_t)g.plane;
+  }
+  __device__ __forceinline__ double *accp(int k) const { return acc + (size_t)k * (size_t)g.plane; }
+};
+
+// Work items per step of one lattice (host and device): an item is one block's
+// WY rows (y) of one x segment (a 64-cell pair segment for the 16-bit kernel)
+// at one level z; items of a lattice are numbered with x fastest, then y, z.
+__host__ __device__ inline long long batch_items(int nx, int ny, int nz, bool pair, int wy) {
+  const int nseg_x = (nx + SEG - 1) / SEG;
+  const int nbx = pair ? (nseg_x + 1) / 2 : nseg_x;
+  return (long long)nbx * ((ny + wy - 1) / wy) * nz;
+}
+
+// Persistent blocks walk the items grid-stride (block b takes b, b + G, ...):
+// items that cost more (the checked path next to stones and the ground) are
+// spread over all blocks, as dynamic block scheduling would spread them.  A
+// lattice has thousands of items, so consecutive items of a block stay in one
+// lattice and the block refills its context only when it crosses into another.
+// The context lives in shared memory (the single-lattice kernel reads the same
+// values from the constant bank) and takes no registers across the item loop.
+template <int DT, bool PAIR, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
+    k_step_batch(const sw_batch_header *__restrict__ hdr, const sw_batch_entry *__restrict__ tab, int k) {
+  __shared__ BatchCtx sc;
+  __shared__ long long s_first, s_next;
+  __shared__ int s_run, s_acc;
+  const long long total = hdr->total_items;
+  long long first = 0, next = 0;                                  // item range of the loaded lattice
+  int nbx = 1, nyb = 1;
+  for (long long item = blockIdx.x; item < total; item += gridDim.x) {
+    if (item >= next || item < first) {                           // uniform across the block
+      __syncthreads();
+      if (threadIdx.x == 0 && threadIdx.y == 0) {
+        const int n = hdr->n;
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (tab[mid].item0 <= item) lo = mid;
+          else hi = mid - 1;
+        }
+        const sw_batch_entry &e = tab[lo];
+        s_first = e.item0;
+        s_next = e.item0 + e.items;
+        s_run = (long long)k < e.steps_left;
+        sc.g.nx = e.geom.nx;
+        sc.g.ny = e.geom.ny;
+        sc.g.nz = e.geom.nz;
+        sc.g.pitch = e.geom.pitch;
+        sc.g.nseg_x = e.geom.pitch / SEG;
+        sc.g.plane = (long long)e.geom.nz * e.geom.ny * e.geom.pitch;
+        const int cur = (e.cur0 + k) & 1;
+        sc.fin = e.f[cur];
+        sc.fout = e.f[cur ^ 1];
+        sc.flag = e.flag;
+        sc.tiles = e.tiles;
+        sc.uin = e.uin;
+        sc.nu0 = e.nu0;
+        sc.cs = e.cs;
+        sc.nu_sponge = e.nu_sponge;
+        sc.x_sponge = e.x_sponge;
+        sc.sponge_scale = (e.geom.nx != e.x_sponge) ? 1.0 / (double)(e.geom.nx - e.x_sponge) : 0.0;
+        const long long t = e.t0 + k;
+        sc.force = e.force ? reinterpret_cast<long long *>(e.force) + t * 2 * e.geom.nz : nullptr;
+        sc.acc = e.acc;
+        s_acc = e.acc != nullptr && t >= e.n_spin && (t - e.n_spin) % e.acc_every == 0;
+      }
+      __syncthreads();
+      first = s_first;
+      next = s_next;
+      nbx = PAIR ? (sc.g.nseg_x + 1) / 2 : sc.g.nseg_x;
+      nyb = (sc.g.ny + Cfg::WY - 1) / Cfg::WY;
+    }
+    const int local = (int)(item - first);
+    const int bx = local % nbx;
+    const int rest = local / nbx;
+    const int yg = rest % nyb;
+    const int z = rest / nyb;
+    if (s_run) {
+      const int y = yg * Cfg::WY + threadIdx.y;
+      if (y < sc.g.ny) {
+        if constexpr (PAIR) {
+          if (s_acc) step_pair_segment<DT, true>(sc, bx, y, z, threadIdx.x);
+          else step_pair_segment<DT, false>(sc, bx, y, z, threadIdx.x);
+        } else {
+          if (s_acc) step_segment<DT, true>(sc, bx, y, z, threadIdx.x);
+          else step_segment<DT, false>(sc, bx, y, z, threadIdx.x);
+        }
+      }
+    }
+  }
+}
+
+template <int DT, bool PAIR, typename Cfg>
+cudaError_t launch_batch_cfg(const sw_batch_header *hdr, const sw_batch_entry *tab, int k, cudaStream_t s) {
+  static int grid = 0;                                             // SMs x resident blocks, per instantiation
+  if (grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_batch<DT, PAIR, Cfg>, Cfg::THREADS, 0);
+    if (e != cudaSuccess) return e;
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  if (k < 0) return cudaSuccess;                                   // query only: grid size now cached
+  k_step_batch<DT, PAIR, Cfg><<<grid, dim3(32, Cfg::WY), 0, s>>>(hdr, tab, k);
+  return cudaGetLastError();
+}
+
+template <int DT>
+cudaError_t launch_batch(const sw_batch_header *hdr, const sw_batch_entry *tab, int cfg, int k, cudaStream_t s) {
+  switch (cfg) {
+#define SW_CASE(ID, WY, MINB) \
+  case ID: return launch_batch_cfg<DT, false, StepCfg<WY, MINB>>(hdr, tab, k, s);
+    SW_STEP_CONFIGS(SW_CASE)
+#undef SW_CASE
+#define SW_CASE(ID, WY, MINB)                                                     \
+  case ID:                                                                        \
+    if constexpr (is16(DT)) return launch_batch_cfg<DT, true, StepCfg<WY, MINB>>(hdr, tab, k, s); \
+    else return cudaErrorNotSupported;
+    SW_PAIR_CONFIGS(SW_CASE)
+#undef SW_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+// (wy, pair) of a configuration, for sw_batch_prepare.
+inline bool config_shape(int cfg, int *wy, bool *pair) {
+  switch (cfg) {
+#define SW_CASE(ID, WY, MINB) \
+  case ID: *wy = WY; *pair = false; return true;
+    SW_STEP_CONFIGS(SW_CASE)
+#undef SW_CASE
+#define SW_CASE(ID, WY, MINB) \
+  case ID: *wy = WY; *pair = true; return true;
+    SW_PAIR_CONFIGS(SW_CASE)
+#undef SW_CASE
+    default:
+      return false;
+  }
+}
+
+}  // namespace sw

@@ -5,6 +5,7 @@
 #include <cstdio>
 
 #include "sw_aux.cuh"
+#include "sw_batch.cuh"
 #include "sw_step.cuh"
 
 namespace {
@@ -212,6 +213,59 @@ int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *fl
                    sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !acc) return SW_ERR_BAD_ARG;
   return cuda_status(sw::aux_macro(to_geom(g), dtype, f, flag, u, acc, st(s)));
+}
+
+int sw_batch_prepare(sw_batch_entry *entries, int32_t n, int dtype, int cfg, sw_batch_header *hdr) {
+  if (!entries || n <= 0 || !hdr || !dtype_ok(dtype)) return SW_ERR_BAD_ARG;
+  if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
+  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  int wy = 0;
+  bool pair = false;
+  sw::config_shape(cfg, &wy, &pair);
+  long long item0 = 0;
+  for (int i = 0; i < n; ++i) {
+    sw_batch_entry &e = entries[i];
+    if (!geom_ok(&e.geom) || !e.f[0] || !e.f[1] || e.f[0] == e.f[1] || !aligned16(e.f[0]) || !aligned16(e.f[1]))
+      return SW_ERR_BAD_ARG;
+    if (!e.flag || !e.tiles || !e.uin || e.cur0 < 0 || e.cur0 > 1 || e.t0 < 0) return SW_ERR_BAD_ARG;
+    if (e.acc && e.acc_every <= 0) return SW_ERR_BAD_ARG;
+    if (e.geom.nz > 65535) return SW_ERR_BAD_ARG;
+    e.items = sw::batch_items(e.geom.nx, e.geom.ny, e.geom.nz, pair, wy);
+    e.item0 = item0;
+    item0 += e.items;
+  }
+  hdr->n = n;
+  hdr->reserved = 0;
+  hdr->total_items = item0;
+  return SW_OK;
+}
+
+int sw_batch_setup(int dtype, int cfg) {
+  if (!dtype_ok(dtype) || cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
+  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  cudaError_t e;
+  switch (dtype) {
+    case SW_F32: e = sw::batch_f32(nullptr, nullptr, cfg, -1, nullptr); break;
+    case SW_F64: e = sw::batch_f64(nullptr, nullptr, cfg, -1, nullptr); break;
+    case SW_F16_SHIFT: e = sw::batch_f16s(nullptr, nullptr, cfg, -1, nullptr); break;
+    default: e = sw::batch_bf16s(nullptr, nullptr, cfg, -1, nullptr); break;
+  }
+  return cuda_status(e);
+}
+
+int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_dev, int dtype, int cfg, int32_t k,
+                  sw_stream s) {
+  if (!hdr_dev || !table_dev || !dtype_ok(dtype) || k < 0) return SW_ERR_BAD_ARG;
+  if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
+  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  cudaError_t e;
+  switch (dtype) {
+    case SW_F32: e = sw::batch_f32(hdr_dev, table_dev, cfg, k, st(s)); break;
+    case SW_F64: e = sw::batch_f64(hdr_dev, table_dev, cfg, k, st(s)); break;
+    case SW_F16_SHIFT: e = sw::batch_f16s(hdr_dev, table_dev, cfg, k, st(s)); break;
+    default: e = sw::batch_bf16s(hdr_dev, table_dev, cfg, k, st(s)); break;
+  }
+  return cuda_status(e);
 }
 
 int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s) {

@@ -49,6 +49,13 @@ struct StepParams {
   const void *fin_pop[Q];
   void *fout_pop[Q];
   double *acc_pop[4];
+
+  // access used by the cell code (shared with the batched kernel's context)
+  template <typename T> __device__ __forceinline__ const T *in(int pop) const {
+    return static_cast<const T *>(fin_pop[pop]);
+  }
+  template <typename T> __device__ __forceinline__ T *out(int pop) const { return static_cast<T *>(fout_pop[pop]); }
+  __device__ __forceinline__ double *accp(int k) const { return acc_pop[k]; }
 };
 
 // Fills the per-population bases from fin / fout / acc (host side).
@@ -172,16 +179,16 @@ constexpr int kStepConfigs = 8;
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
 // tests (segments next to stones, the ground or a fluid cell at z = 0).
 // Offsets within a population plane are 32-bit (grids below 2^31 cells).
-template <int DT, bool CHECK, bool ACC>
-__device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int z, typename Store<DT>::R &fxw,
+template <int DT, bool CHECK, bool ACC, typename Ctx>
+__device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typename Store<DT>::R &fxw,
                                           typename Store<DT>::R &fzw, int &hit) {
   using S = Store<DT>;
   using T = typename S::T;
   using R = typename S::R;
   const Geom &g = p.g;
   const int c = (z * g.ny + y) * g.pitch + x;
-  auto in = [&](int pop) { return static_cast<const T *>(p.fin_pop[pop]); };
-  auto out = [&](int pop) { return static_cast<T *>(p.fout_pop[pop]); };
+  auto in = [&](int pop) { return p.template in<T>(pop); };
+  auto out = [&](int pop) { return p.template out<T>(pop); };
   if (CHECK && p.flag[c] != 0) return;                          // lbm3d.py:65-66
   if (x == 0) {                                                 // inlet, lbm3d.py:67-71
     const R u0 = (R)__ldg(p.uin + z);
@@ -196,8 +203,8 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
       S::template st<i>(out(i) + c, S::kShift ? v - W<R>(i) : v);
     });
     if (ACC) {
-      atomicAdd(p.acc_pop[0] + c, 1.0);
-      atomicAdd(p.acc_pop[1] + c, (double)u0);
+      atomicAdd(p.accp(0) + c, 1.0);
+      atomicAdd(p.accp(1) + c, (double)u0);
     }
     return;
   }
@@ -251,17 +258,17 @@ __device__ __forceinline__ void step_cell(const StepParams &p, int x, int y, int
                           S::template st<i>(out(i) + c, v);
                         });
   if (ACC) {  // each cell is owned by one thread: reductions without a return value (no read stall)
-    atomicAdd(p.acc_pop[0] + c, (double)rho);
-    atomicAdd(p.acc_pop[1] + c, (double)ux);
-    atomicAdd(p.acc_pop[2] + c, (double)uy);
-    atomicAdd(p.acc_pop[3] + c, (double)uz);
+    atomicAdd(p.accp(0) + c, (double)rho);
+    atomicAdd(p.accp(1) + c, (double)ux);
+    atomicAdd(p.accp(2) + c, (double)uy);
+    atomicAdd(p.accp(3) + c, (double)uz);
   }
 }
 
 // Adds the warp's wall force (lbm3d.py:99-101): float64 xor-butterfly sum, then
 // one 2^-40 fixed-point integer atomic per component.
-template <typename R>
-__device__ __forceinline__ void warp_force_add(const StepParams &p, int z, int lane, R fxw, R fzw, int hit) {
+template <typename R, typename Ctx>
+__device__ __forceinline__ void warp_force_add(const Ctx &p, int z, int lane, R fxw, R fzw, int hit) {
   double dx = (double)fxw, dz = (double)fzw;
   const unsigned any = __ballot_sync(0xffffffffu, hit);
 #pragma unroll
@@ -277,19 +284,15 @@ __device__ __forceinline__ void warp_force_add(const StepParams &p, int z, int l
   }
 }
 
-// Grid: (pitch / 32, ceil(ny / WY), nz); warp (threadIdx.y) = one row segment.
-template <int DT, bool ACC, typename Cfg>
-__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(const __grid_constant__ StepParams p) {
+// One warp, one 32-cell row segment (sx, y, z): fast path, checked path or nothing.
+template <int DT, bool ACC, typename Ctx>
+__device__ __forceinline__ void step_segment(const Ctx &p, int sx, int y, int z, int lane) {
   using R = typename Store<DT>::R;
   const Geom &g = p.g;
-  const int y = blockIdx.y * Cfg::WY + threadIdx.y;
-  if (y >= g.ny) return;
-  const int z = blockIdx.z;
-  const int lane = threadIdx.x;
-  const int seg = (z * g.ny + y) * g.nseg_x + blockIdx.x;
+  const int seg = (z * g.ny + y) * g.nseg_x + sx;
   const uint8_t kind = __ldg(p.tiles + seg);
   if (kind & TILE_ALL_SOLID) return;
-  const int x = blockIdx.x * SEG + lane;
+  const int x = sx * SEG + lane;
   R fxw = R(0.0), fzw = R(0.0);
   int hit = 0;
   if (!(kind & TILE_CHECK)) {
@@ -298,6 +301,14 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(const __g
   }
   if (x < g.nx) step_cell<DT, true, ACC>(p, x, y, z, fxw, fzw, hit);
   if ((kind & TILE_FORCE) && p.force != nullptr) warp_force_add<R>(p, z, lane, fxw, fzw, hit);
+}
+
+// Grid: (pitch / 32, ceil(ny / WY), nz); warp (threadIdx.y) = one row segment.
+template <int DT, bool ACC, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(const __grid_constant__ StepParams p) {
+  const int y = blockIdx.y * Cfg::WY + threadIdx.y;
+  if (y >= p.g.ny) return;
+  step_segment<DT, ACC>(p, blockIdx.x, y, (int)blockIdx.z, threadIdx.x);
 }
 
 // ---------------------------------------------------------------- two cells per thread, 16-bit storage
@@ -327,8 +338,8 @@ template <> struct Pack16<SW_BF16_SHIFT> {
   }
 };
 
-template <int DT, bool ACC>
-__device__ __forceinline__ void step_pair_fast(const StepParams &p, int x0, int y, int z, int lane) {
+template <int DT, bool ACC, typename Ctx>
+__device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int z, int lane) {
   using S = Store<DT>;
   using T = typename S::T;
   using PK = Pack16<DT>;
@@ -337,8 +348,8 @@ __device__ __forceinline__ void step_pair_fast(const StepParams &p, int x0, int 
   const bool has_b = x0 + 1 < g.nx;   // cell x0 + 1 exists
   const bool has_r = x0 + 2 < g.nx;   // cell x0 + 2 exists (else the outlet copies x0 + 1)
   const int c = (z * g.ny + y) * g.pitch + x0;
-  auto in = [&](int pop) { return static_cast<const T *>(p.fin_pop[pop]); };
-  auto out = [&](int pop) { return static_cast<T *>(p.fout_pop[pop]); };
+  auto in = [&](int pop) { return p.template in<T>(pop); };
+  auto out = [&](int pop) { return p.template out<T>(pop); };
   const int row = g.pitch, lev = g.ny * g.pitch;
   const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
   const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
@@ -407,34 +418,30 @@ __device__ __forceinline__ void step_pair_fast(const StepParams &p, int x0, int 
                          else __stcs(out(i) + c, oa[i]);
                        });
   if (ACC) {
-    atomicAdd(p.acc_pop[0] + c, (double)ra);
-    atomicAdd(p.acc_pop[1] + c, (double)uxa);
-    atomicAdd(p.acc_pop[2] + c, (double)uya);
-    atomicAdd(p.acc_pop[3] + c, (double)uza);
+    atomicAdd(p.accp(0) + c, (double)ra);
+    atomicAdd(p.accp(1) + c, (double)uxa);
+    atomicAdd(p.accp(2) + c, (double)uya);
+    atomicAdd(p.accp(3) + c, (double)uza);
     if (has_b) {
-      atomicAdd(p.acc_pop[0] + c + 1, (double)rb);
-      atomicAdd(p.acc_pop[1] + c + 1, (double)uxb);
-      atomicAdd(p.acc_pop[2] + c + 1, (double)uyb);
-      atomicAdd(p.acc_pop[3] + c + 1, (double)uzb);
+      atomicAdd(p.accp(0) + c + 1, (double)rb);
+      atomicAdd(p.accp(1) + c + 1, (double)uxb);
+      atomicAdd(p.accp(2) + c + 1, (double)uyb);
+      atomicAdd(p.accp(3) + c + 1, (double)uzb);
     }
   }
 }
 
-// Grid: (ceil(pitch / 64), ceil(ny / WY), nz); warp = two adjacent row segments.
-template <int DT, bool ACC, typename Cfg>
-__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pair(const __grid_constant__ StepParams p) {
+// One warp, the row segments 2 bx and 2 bx + 1 of (y, z).
+template <int DT, bool ACC, typename Ctx>
+__device__ __forceinline__ void step_pair_segment(const Ctx &p, int bx, int y, int z, int lane) {
   const Geom &g = p.g;
-  const int y = blockIdx.y * Cfg::WY + threadIdx.y;
-  if (y >= g.ny) return;
-  const int z = blockIdx.z;
-  const int lane = threadIdx.x;
-  const int sa = 2 * blockIdx.x;
+  const int sa = 2 * bx;
   const bool has_tb = sa + 1 < g.nseg_x;
   const int seg = (z * g.ny + y) * g.nseg_x + sa;
   const uint8_t ka = __ldg(p.tiles + seg);
   const uint8_t kb = has_tb ? __ldg(p.tiles + seg + 1) : (uint8_t)TILE_ALL_SOLID;
   if ((ka & kb & TILE_ALL_SOLID)) return;
-  const int x0 = 2 * SEG * blockIdx.x + 2 * lane;
+  const int x0 = 2 * SEG * bx + 2 * lane;
   if (!((ka | kb) & TILE_CHECK)) {
     step_pair_fast<DT, ACC>(p, x0, y, z, lane);
     return;
@@ -444,6 +451,14 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pair(const __g
   if (x0 < g.nx) step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
   if (x0 + 1 < g.nx) step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
   if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+}
+
+// Grid: (ceil(pitch / 64), ceil(ny / WY), nz); warp = two adjacent row segments.
+template <int DT, bool ACC, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pair(const __grid_constant__ StepParams p) {
+  const int y = blockIdx.y * Cfg::WY + threadIdx.y;
+  if (y >= p.g.ny) return;
+  step_pair_segment<DT, ACC>(p, blockIdx.x, y, (int)blockIdx.z, threadIdx.x);
 }
 
 template <int DT, bool ACC, typename Cfg>

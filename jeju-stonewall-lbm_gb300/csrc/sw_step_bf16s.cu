@@ -1,7 +1,11 @@
-// sw_step_bf16s.cu -- instantiation of the fused step for storage type SW_BF16_SHIFT.
+// sw_step_bf16s.cu -- instantiations of the fused step (single lattice and batched) for SW_BF16_SHIFT.
 #include "sw_aux.cuh"
+#include "sw_batch.cuh"
 #include "sw_step.cuh"
 
 namespace sw {
 cudaError_t step_bf16s(const StepParams &p, cudaStream_t s) { return launch_step<SW_BF16_SHIFT>(p, s); }
+cudaError_t batch_bf16s(const sw_batch_header *h, const sw_batch_entry *t, int cfg, int k, cudaStream_t s) {
+  return launch_batch<SW_BF16_SHIFT>(h, t, cfg, k, s);
+}
 }  // namespace sw

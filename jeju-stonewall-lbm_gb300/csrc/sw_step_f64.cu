@@ -1,7 +1,11 @@
-// sw_step_f64.cu -- instantiation of the fused step for storage type SW_F64.
+// sw_step_f64.cu -- instantiations of the fused step (single lattice and batched) for SW_F64.
 #include "sw_aux.cuh"
+#include "sw_batch.cuh"
 #include "sw_step.cuh"
 
 namespace sw {
 cudaError_t step_f64(const StepParams &p, cudaStream_t s) { return launch_step<SW_F64>(p, s); }
+cudaError_t batch_f64(const sw_batch_header *h, const sw_batch_entry *t, int cfg, int k, cudaStream_t s) {
+  return launch_batch<SW_F64>(h, t, cfg, k, s);
+}
 }  // namespace sw

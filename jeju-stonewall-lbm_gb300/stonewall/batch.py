@@ -1,0 +1,212 @@
+"""Batch: many wall solves advanced together, one persistent launch per step.
+
+Each member is a WallSolver (its own buffers, mask, inlet, force series and
+sums); the batch keeps a table describing all members in device memory
+(sw_batch_entry, include/stonewall.h) and launches sw_batch_step, which walks
+every member's work in one grid of (SMs x resident blocks).  Runs of `chunk`
+steps are replayed from a CUDA graph captured once per chunk size: the kernel
+reads the table when it runs, so between replays the host only rewrites each
+member's step counter, remaining steps and current buffer (and, for serving,
+adds or drops members).  All members share one storage type.
+
+A member's results do not depend on the others (cells are owned by one
+thread, wall forces are integer sums), so a wall gives the same bits alone
+and in any mix; tests/test_gpu_batch.py checks this.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .fields import _stream
+
+
+class SwBatchEntry(ctypes.Structure):
+    _fields_ = [("geom", N.SwGeom), ("item0", ctypes.c_int64), ("items", ctypes.c_int64),
+                ("f", ctypes.c_void_p * 2), ("flag", ctypes.c_void_p), ("tiles", ctypes.c_void_p),
+                ("uin", ctypes.c_void_p), ("force", ctypes.c_void_p), ("acc", ctypes.c_void_p),
+                ("nu0", ctypes.c_double), ("cs", ctypes.c_double), ("nu_sponge", ctypes.c_double),
+                ("x_sponge", ctypes.c_int32), ("n_spin", ctypes.c_int32), ("acc_every", ctypes.c_int32),
+                ("cur0", ctypes.c_int32), ("t0", ctypes.c_int64), ("steps_left", ctypes.c_int64)]
+
+
+class SwBatchHeader(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("reserved", ctypes.c_int32), ("total_items", ctypes.c_int64)]
+
+
+def _bind():
+    L = N.lib()
+    if not hasattr(L.sw_batch_prepare, "_sw_bound"):
+        P = ctypes.c_void_p
+        L.sw_batch_prepare.argtypes = [P, ctypes.c_int32, ctypes.c_int, ctypes.c_int, P]
+        L.sw_batch_prepare.restype = ctypes.c_int
+        L.sw_batch_step.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int32, P]
+        L.sw_batch_step.restype = ctypes.c_int
+        L.sw_batch_setup.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.sw_batch_setup.restype = ctypes.c_int
+        L.sw_batch_prepare._sw_bound = True
+    return L
+
+
+def acc_steps(t0, n, n_spin, every):
+    """How many of the steps t0 .. t0+n-1 accumulate (t >= n_spin, (t - n_spin) % every == 0)."""
+    lo = max(t0, n_spin)
+    hi = t0 + n
+    if hi <= lo:
+        return 0
+    first = lo + (-(lo - n_spin)) % every
+    return 0 if first >= hi else (hi - 1 - first) // every + 1
+
+
+class Batch:
+    def __init__(self, dtype="f16", device="cuda", chunk=50, max_members=512, cfg=None):
+        self.dtype = N.dtype_code(dtype)
+        self.device = torch.device(device)
+        self.chunk = int(chunk)
+        self.max_members = int(max_members)
+        self.members = []
+        self.cfg = cfg if cfg is not None else (4 if self.dtype in (N.SW_F16_SHIFT, N.SW_BF16_SHIFT) else 3)
+        esz = ctypes.sizeof(SwBatchEntry)
+        self._table_dev = torch.zeros(self.max_members * esz, dtype=torch.uint8, device=self.device)
+        self._hdr_dev = torch.zeros(ctypes.sizeof(SwBatchHeader), dtype=torch.uint8, device=self.device)
+        # two pinned host copies, alternated so that one can be rewritten while the other uploads
+        self._table_host = [(SwBatchEntry * self.max_members)() for _ in range(2)]
+        self._hdr_host = [SwBatchHeader() for _ in range(2)]
+        self._pinned = [torch.empty(self.max_members * esz + ctypes.sizeof(SwBatchHeader), dtype=torch.uint8)
+                        .pin_memory() for _ in range(2)]
+        self._upload_done = [None, None]
+        self._slot = 0
+        self._graphs = {}
+        self.launches = 0
+        _bind()
+
+    # ------------------------------------------------------------ membership
+    def add(self, solver):
+        if solver.dtype != self.dtype:
+            raise ValueError("all members of a batch share one storage type")
+        if len(self.members) >= self.max_members:
+            raise RuntimeError("batch is full")
+        self.members.append(solver)
+        return solver
+
+    def remove(self, solver):
+        self.members = [m for m in self.members if m is not solver]
+
+    def pending(self):
+        return [m for m in self.members if m.t < m.n_total]
+
+    # ------------------------------------------------------------ table
+    def _fill(self, n_steps, tuning=False):
+        slot = self._slot
+        self._slot ^= 1
+        if self._upload_done[slot] is not None:
+            self._upload_done[slot].synchronize()
+        tab, hdr = self._table_host[slot], self._hdr_host[slot]
+        live = [m for m in self.members if m.t < m.n_total]
+        for i, m in enumerate(live):
+            e = tab[i]
+            e.geom = m.grid.geom
+            e.f[0] = m.f[0].data.data_ptr()
+            e.f[1] = m.f[1].data.data_ptr()
+            e.flag = m.flags.flag.data_ptr()
+            e.tiles = m.flags.tiles.data_ptr()
+            e.uin = m.uin.data.data_ptr()
+            e.force = None if tuning else m.force.data.data_ptr()
+            e.acc = None if tuning else m.acc.data.data_ptr()
+            e.nu0, e.cs, e.nu_sponge = m.nu0, m.cs, m.nu_sponge
+            e.x_sponge, e.n_spin, e.acc_every, e.cur0 = m.x_sponge, m.n_spin, m.acc_every, m.cur
+            e.t0 = m.t
+            e.steps_left = min(n_steps, m.n_total - m.t)
+        if not live:
+            return slot, live
+        N.check(N.lib().sw_batch_prepare(ctypes.byref(tab), len(live), self.dtype, self.cfg, ctypes.byref(hdr)),
+                "sw_batch_prepare")
+        esz = ctypes.sizeof(SwBatchEntry)
+        buf = self._pinned[slot]
+        nbytes = len(live) * esz
+        ctypes.memmove(buf.data_ptr(), ctypes.addressof(tab), nbytes)
+        ctypes.memmove(buf.data_ptr() + self.max_members * esz, ctypes.addressof(hdr), ctypes.sizeof(hdr))
+        self._table_dev[:nbytes].copy_(buf[:nbytes], non_blocking=True)
+        self._hdr_dev.copy_(buf[self.max_members * esz:], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        self._upload_done[slot] = ev
+        return slot, live
+
+    def _launch(self, k):
+        N.check(N.lib().sw_batch_step(ctypes.c_void_p(self._hdr_dev.data_ptr()),
+                                      ctypes.c_void_p(self._table_dev.data_ptr()), self.dtype, self.cfg, int(k),
+                                      _stream(None)), "sw_batch_step")
+
+    def _graph(self, n):
+        key = (n, self.cfg)
+        if key not in self._graphs:
+            N.check(N.lib().sw_batch_setup(self.dtype, self.cfg), "sw_batch_setup")   # no device queries in capture
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                for k in range(n):
+                    self._launch(k)
+            self._graphs[key] = g
+        return self._graphs[key]
+
+    # ------------------------------------------------------------ stepping
+    def advance(self, n, use_graphs=True):
+        """Advance every unfinished member by up to n steps (each stops at its own n_total)."""
+        n = int(n)
+        while n > 0:
+            c = min(self.chunk, n)
+            slot, live = self._fill(c)
+            if not live:
+                return self
+            if use_graphs and c == self.chunk:
+                self._graph(c).replay()
+            else:
+                for k in range(c):
+                    self._launch(k)
+            self.launches += c
+            for m in live:
+                s = min(c, m.n_total - m.t)
+                m.n_acc += acc_steps(m.t, s, m.n_spin, m.acc_every)
+                m.t += s
+                m.cur ^= (s & 1)
+            n -= c
+        return self
+
+    def run(self):
+        """Advance until every member has finished."""
+        while self.pending():
+            self.advance(self.chunk * 20)
+        return self
+
+    def cells(self):
+        return sum(m.grid.cells for m in self.members)
+
+    def autotune(self, repeats=5):
+        """Time every configuration this storage type has on the current members and keep the
+        fastest.  Each timing launch recomputes every member's next state into its spare
+        buffer with forces and sums switched off, so the members' states are not changed."""
+        best, times = None, {}
+        for cfg in range(N.lib().sw_step_config_count()):
+            if not _valid(self.dtype, cfg):
+                continue
+            self.cfg = cfg
+            self._fill(1, tuning=True)
+            self._launch(0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(repeats):
+                self._launch(0)
+            e1.record()
+            torch.cuda.synchronize()
+            times[cfg] = e0.elapsed_time(e1) / repeats
+            if best is None or times[cfg] < times[best]:
+                best = cfg
+        self.cfg = best
+        return best, times
+
+
+def _valid(dtype, cfg):
+    return cfg < 4 or dtype in (N.SW_F16_SHIFT, N.SW_BF16_SHIFT)
