@@ -1,0 +1,254 @@
+"""Continuous-batching solve server: wall-design requests in, wall-load statistics out.
+
+    python -m stonewall.serve [--minutes 30] [--rate 2] [--cap-gb 160] [--seed 0] ...
+
+Requests arrive as a Poisson process (seeded).  Each asks for one wall: H
+from U{H_lo..H_hi}, porosity U[0, 0.5], inlet speed U_H U[0.03, 0.06], a step
+budget U[5000, 40000], a fresh seeded ellipsoid-packed stone mask, and a
+storage type (fp32 or fp16-shifted, by a seeded coin).  The server:
+
+  * builds masks on host threads while requests wait (CPU work off the loop);
+  * admits queued requests first-come first-served while their device
+    footprint (both lattices, flags, sums, force series) fits under the cap;
+  * keeps every admitted solve resident and advances all of them together:
+    one Batch per storage type, each replaying a captured graph of `chunk`
+    persistent launches per loop iteration, so requests that arrive while
+    others run join at the next chunk boundary;
+  * retires finished solves (force series -> Cd, Cm statistics), frees their
+    memory and admits more.
+
+Reported: p50 / p99 time-to-result (arrival to result), queueing and run
+times, solves per hour over the run, GPU throughput.  A solve's result does
+not depend on what it shared the GPU with (see stonewall.batch).
+"""
+import argparse
+import concurrent.futures as cf
+import json
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .batch import Batch
+from .geometry import ellipsoid_wall
+from .metrics import coefficients, stats
+from .params import baseline_params, flags_from_wall
+from .solver import WallSolver
+
+DTYPE_BYTES = {"f32": 4, "f16": 2, "bf16": 2, "f64": 8}
+
+
+@dataclass
+class Request:
+    rid: int
+    t_arrive: float
+    H: int
+    porosity: float
+    U: float
+    steps: int
+    dtype: str
+    seed: int
+    result: dict = field(default=None)
+
+
+def poisson_requests(rate, duration, seed=0, H_range=(16, 48), porosity=(0.0, 0.5), U=(0.03, 0.06),
+                     steps=(5000, 40000), f16_share=0.5):
+    """Requests with exponential inter-arrival times (mean 1/rate) over [0, duration) seconds."""
+    rng = np.random.default_rng(seed)
+    out, t, rid = [], 0.0, 0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= duration:
+            return out
+        out.append(Request(rid=rid, t_arrive=t, H=int(rng.integers(H_range[0], H_range[1] + 1)),
+                           porosity=float(rng.uniform(*porosity)), U=float(rng.uniform(*U)),
+                           steps=int(rng.integers(steps[0], steps[1] + 1)),
+                           dtype="f16" if rng.random() < f16_share else "f32", seed=1000 + rid))
+        rid += 1
+
+
+def footprint(req):
+    """Device bytes a request holds while resident."""
+    p = baseline_params(req.H, req.steps, UH=req.U)
+    pitch = (p.nx + 31) // 32 * 32
+    cells = pitch * p.ny * p.nz
+    return (2 * 19 * DTYPE_BYTES[req.dtype] * cells + 32 * cells + cells + cells // 32 + req.steps * p.nz * 16
+            + p.nz * 4)
+
+
+def prepare(req):
+    """Host side of a request: parameters and the flag array (run on a worker thread)."""
+    p = baseline_params(req.H, req.steps, UH=req.U)
+    wall, frac = ellipsoid_wall(req.porosity, p.H, p.nx, p.ny, p.nz, p.X0, p.T, seed=req.seed)
+    return p, flags_from_wall(wall, p.nx, p.ny, p.nz)
+
+
+def make_solver(req, p, flag, device="cuda"):
+    s = WallSolver(flag, p.uin, p.nu0, p.Cs, p.x_sponge, req.steps, n_spin=p.n_spin, dtype=req.dtype,
+                   device=device)
+    s.init(noise=0.02, seed=req.seed, noise_kind="gauss")
+    s.params = p
+    return s
+
+
+def solve_stats(s):
+    p = s.params
+    co = coefficients(s.force_series(), p.UH, p.H, p.ny)
+    return stats(co["Cd"], co["Cm"], co["Cl"], s.n_spin)
+
+
+class Server:
+    def __init__(self, cap_bytes=160e9, chunk=50, max_members=256, device="cuda", workers=4, clock=time.monotonic):
+        self.cap = float(cap_bytes)
+        self.chunk = int(chunk)
+        self.device = torch.device(device)
+        self.batches = {dt: Batch(dtype=dt, chunk=chunk, max_members=max_members, device=device)
+                        for dt in ("f32", "f16")}
+        self.pool = cf.ThreadPoolExecutor(max_workers=workers)
+        self.clock = clock
+        self.resident = {}                         # rid -> (request, solver, bytes)
+        self.used = 0.0
+        self.log = []
+
+    def _admit(self, queue, prepared, now):
+        while queue:
+            req = queue[0]
+            fut = prepared.get(req.rid)
+            if fut is None or not fut.done():
+                return                               # head still being prepared: keep FIFO order
+            need = footprint(req)
+            if need > self.cap:
+                raise ValueError(f"request {req.rid} needs {need/1e9:.1f} GB, more than the cap")
+            if self.used + need > self.cap:
+                return
+            queue.pop(0)
+            p, flag = fut.result()
+            del prepared[req.rid]
+            s = make_solver(req, p, flag, self.device)
+            self.batches[req.dtype].add(s)
+            self.resident[req.rid] = (req, s, need)
+            self.used += need
+            req.t_admit = now
+
+    def _retire(self, now):
+        done = [rid for rid, (req, s, need) in self.resident.items() if s.t >= s.n_total]
+        for rid in done:
+            req, s, need = self.resident.pop(rid)
+            st = solve_stats(s)
+            req.result = dict(stats=st, t_done=now, latency=now - req.t_arrive, wait=req.t_admit - req.t_arrive,
+                              run=now - req.t_admit, cells=s.grid.cells)
+            self.batches[req.dtype].remove(s)
+            self.used -= need
+            del s
+        return len(done)
+
+    def serve(self, requests, max_seconds=None, drain=True, log_every=30.0):
+        """Replay the request stream in real time.  Returns the requests (with .result when done)."""
+        reqs = sorted(requests, key=lambda r: r.t_arrive)
+        queue, prepared = [], {}
+        t0 = self.clock()
+        i = 0
+        last_log = 0.0
+        self.max_used = 0.0
+        while True:
+            now = self.clock() - t0
+            while i < len(reqs) and reqs[i].t_arrive <= now:
+                queue.append(reqs[i])
+                prepared[reqs[i].rid] = self.pool.submit(prepare, reqs[i])
+                i += 1
+            self._admit(queue, prepared, now)
+            active = [b for b in self.batches.values() if b.pending()]
+            self.max_used = max(self.max_used, self.used)
+            if active:
+                for b in active:
+                    b.advance(self.chunk)
+                torch.cuda.synchronize()
+            else:
+                if i >= len(reqs) and not queue:
+                    break
+                time.sleep(0.005)
+            now = self.clock() - t0
+            self._retire(now)
+            if max_seconds is not None and now > max_seconds and not drain:
+                break
+            if max_seconds is not None and now > max_seconds and drain and i < len(reqs):
+                reqs = reqs[:i]                          # stop accepting new arrivals, finish the rest
+            if now - last_log > log_every:
+                last_log = now
+                self.log.append(dict(t=round(now, 1), resident=len(self.resident), queued=len(queue),
+                                     used_gb=round(self.used / 1e9, 1),
+                                     done=sum(1 for r in reqs[:i] if r.result is not None)))
+        self.pool.shutdown(wait=False)
+        self.unfinished = dict(queued=len(queue), resident=len(self.resident))
+        return reqs
+
+    @staticmethod
+    def summary(reqs, elapsed):
+        done = [r for r in reqs if r.result is not None]
+        lat = np.array([r.result["latency"] for r in done]) if done else np.zeros(1)
+        wait = np.array([r.result["wait"] for r in done]) if done else np.zeros(1)
+        cell_steps = sum(r.result["cells"] * r.steps for r in done)
+        return dict(requests=len(reqs), completed=len(done), elapsed_s=round(elapsed, 1),
+                    solves_per_hour=round(len(done) / elapsed * 3600, 1) if elapsed > 0 else 0.0,
+                    p50_latency_s=round(float(np.percentile(lat, 50)), 2),
+                    p99_latency_s=round(float(np.percentile(lat, 99)), 2),
+                    p50_wait_s=round(float(np.percentile(wait, 50)), 2),
+                    mean_glups=round(cell_steps / elapsed / 1e9, 2) if elapsed > 0 else 0.0,
+                    f16_share=round(np.mean([r.dtype == "f16" for r in done]), 3) if done else 0.0)
+
+
+def run_alone(req, device="cuda"):
+    """The same request solved by itself (its own batch), for alone-vs-mix checks and FP64 references."""
+    p, flag = prepare(req)
+    s = make_solver(req, p, flag, device)
+    b = Batch(dtype=req.dtype, chunk=50, max_members=4, device=device)
+    b.add(s)
+    b.run()
+    return s
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--minutes", type=float, default=30.0, help="arrival window")
+    ap.add_argument("--rate", type=float, default=2.0, help="mean arrivals per second")
+    ap.add_argument("--cap-gb", type=float, default=160.0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--h-lo", type=int, default=16)
+    ap.add_argument("--h-hi", type=int, default=48)
+    ap.add_argument("--steps-lo", type=int, default=5000)
+    ap.add_argument("--steps-hi", type=int, default=40000)
+    ap.add_argument("--f16-share", type=float, default=0.5)
+    ap.add_argument("--chunk", type=int, default=50)
+    ap.add_argument("--no-drain", action="store_true", help="stop at the end of the window (unfinished solves count as not done)")
+    ap.add_argument("--fp64-check", type=int, default=0, help="re-run this many completed requests in float64")
+    a = ap.parse_args(argv)
+    reqs = poisson_requests(a.rate, a.minutes * 60.0, seed=a.seed, H_range=(a.h_lo, a.h_hi),
+                            steps=(a.steps_lo, a.steps_hi), f16_share=a.f16_share)
+    srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk)
+    t0 = time.monotonic()
+    out = srv.serve(reqs, max_seconds=a.minutes * 60.0, drain=not a.no_drain)
+    elapsed = time.monotonic() - t0
+    summ = srv.summary(out, elapsed)
+    summ.update(unfinished_at_end=srv.unfinished, max_resident_gb=round(srv.max_used / 1e9, 2), cap_gb=a.cap_gb,
+                arrivals_per_s=a.rate, window_minutes=a.minutes)
+    if a.fp64_check:
+        done = sorted([r for r in out if r.result is not None], key=lambda r: r.H * r.steps)[:a.fp64_check]
+        errs = []
+        for r in done:
+            ref = run_alone(Request(rid=r.rid, t_arrive=r.t_arrive, H=r.H, porosity=r.porosity, U=r.U, steps=r.steps,
+                                    dtype="f64", seed=r.seed))
+            rs = solve_stats(ref)
+            errs.append(dict(rid=r.rid, dtype=r.dtype, H=r.H,
+                             Cd=abs(r.result["stats"]["Cd"] - rs["Cd"]) / abs(rs["Cd"]),
+                             CdMax=abs(r.result["stats"]["CdMax"] - rs["CdMax"]) / abs(rs["CdMax"])))
+            del ref
+            torch.cuda.empty_cache()
+        summ["fp64_check"] = errs
+    summ["log"] = srv.log[-10:]
+    print(json.dumps(summ), flush=True)
+    return summ
+
+
+if __name__ == "__main__":
+    main()

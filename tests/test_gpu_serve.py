@@ -1,0 +1,42 @@
+"""The solve server: admission under a memory cap, continuous batching, alone vs in the mix.
+
+Small walls (H 8..12) and short budgets keep this to seconds; the cap is set so
+that only a few solves fit at once and the others wait in the queue.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    from stonewall.serve import poisson_requests
+    return poisson_requests(rate=20.0, duration=0.6, seed=3, H_range=(8, 12), steps=(60, 200), f16_share=0.5)
+
+
+def test_server_completes_everything_under_the_cap(cuda):
+    from stonewall.serve import Server, footprint
+    reqs = _requests()
+    assert len(reqs) >= 6 and {r.dtype for r in reqs} == {"f32", "f16"}
+    cap = 2.5 * max(footprint(r) for r in reqs)
+    srv = Server(cap_bytes=cap, chunk=16)
+    out = srv.serve(reqs)
+    assert all(r.result is not None for r in out)
+    assert srv.max_used <= cap
+    assert srv.used == 0 and not srv.resident
+    admits = sorted(out, key=lambda r: r.t_admit)
+    assert [r.rid for r in admits] == [r.rid for r in sorted(out, key=lambda r: r.t_arrive)]   # first come first served
+    summ = Server.summary(out, 10.0)
+    assert summ["completed"] == len(reqs) and summ["p99_latency_s"] >= summ["p50_latency_s"]
+
+
+def test_result_is_the_same_alone_and_in_the_mix(cuda):
+    from stonewall.serve import Server, run_alone, solve_stats
+    reqs = _requests()
+    srv = Server(cap_bytes=1e12, chunk=16)
+    out = srv.serve(reqs)
+    for r in out[:4]:
+        alone = run_alone(r)
+        st = solve_stats(alone)
+        for k, v in st.items():
+            assert v == r.result["stats"][k] or (np.isnan(v) and np.isnan(r.result["stats"][k])), (r.rid, k)
