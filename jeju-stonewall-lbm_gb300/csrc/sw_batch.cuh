@@ -22,22 +22,20 @@ namespace sw {
 // Cell-code context of one batched lattice: population planes at pop * plane.
 struct BatchCtx {
   Geom g;
-  const void *fin;
-  void *fout;
   const uint8_t *flag;
   const uint8_t *tiles;
   const float *uin;
   double nu0, cs, nu_sponge, sponge_scale;
   int x_sponge;
   long long *force;
-  double *acc;
+  const void *fin_pop[Q];   // plane bases, filled once per lattice
+  void *fout_pop[Q];
+  double *acc_pop[4];
   template <typename T> __device__ __forceinline__ const T *in(int pop) const {
-    return static_cast<const T *>(fin) + (size_t)pop * (size_t)g.plane;
+    return static_cast<const T *>(fin_pop[pop]);
   }
-  template <typename T> __device__ __forceinline__ T *out(int pop) const {
-    return static_cast<T *>(fout) + (size_t)pop * (size_t)g.plane;
-  }
-  __device__ __forceinline__ double *accp(int k) const { return acc + (size_t)k * (size_t)g.plane; }
+  template <typename T> __device__ __forceinline__ T *out(int pop) const { return static_cast<T *>(fout_pop[pop]); }
+  __device__ __forceinline__ double *accp(int k) const { return acc_pop[k]; }
 };
 
 // Work items per step of one lattice (host and device): an item is one block's
@@ -61,7 +59,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     k_step_batch(const sw_batch_header *__restrict__ hdr, const sw_batch_entry *__restrict__ tab, int k) {
   __shared__ BatchCtx sc;
   __shared__ long long s_first, s_next;
-  __shared__ int s_run, s_acc;
+  __shared__ int s_run, s_acc, s_lat;
   const long long total = hdr->total_items;
   long long first = 0, next = 0;                                  // item range of the loaded lattice
   int nbx = 1, nyb = 1;
@@ -77,6 +75,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
           else hi = mid - 1;
         }
         const sw_batch_entry &e = tab[lo];
+        s_lat = lo;
         s_first = e.item0;
         s_next = e.item0 + e.items;
         s_run = (long long)k < e.steps_left;
@@ -86,9 +85,6 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
         sc.g.pitch = e.geom.pitch;
         sc.g.nseg_x = e.geom.pitch / SEG;
         sc.g.plane = (long long)e.geom.nz * e.geom.ny * e.geom.pitch;
-        const int cur = (e.cur0 + k) & 1;
-        sc.fin = e.f[cur];
-        sc.fout = e.f[cur ^ 1];
         sc.flag = e.flag;
         sc.tiles = e.tiles;
         sc.uin = e.uin;
@@ -99,8 +95,17 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
         sc.sponge_scale = (e.geom.nx != e.x_sponge) ? 1.0 / (double)(e.geom.nx - e.x_sponge) : 0.0;
         const long long t = e.t0 + k;
         sc.force = e.force ? reinterpret_cast<long long *>(e.force) + t * 2 * e.geom.nz : nullptr;
-        sc.acc = e.acc;
         s_acc = e.acc != nullptr && t >= e.n_spin && (t - e.n_spin) % e.acc_every == 0;
+      }
+      __syncthreads();
+      {                                                           // plane bases, one per thread
+        const sw_batch_entry &e = tab[s_lat];
+        const int tid = threadIdx.y * 32 + threadIdx.x;
+        const int cur = (e.cur0 + k) & 1;
+        const size_t pb = (size_t)sc.g.plane * sizeof(typename Store<DT>::T);
+        if (tid < Q) sc.fin_pop[tid] = static_cast<const char *>(e.f[cur]) + tid * pb;
+        else if (tid < 2 * Q) sc.fout_pop[tid - Q] = static_cast<char *>(e.f[cur ^ 1]) + (tid - Q) * pb;
+        else if (tid < 2 * Q + 4) sc.acc_pop[tid - 2 * Q] = e.acc ? e.acc + (size_t)(tid - 2 * Q) * sc.g.plane : nullptr;
       }
       __syncthreads();
       first = s_first;
