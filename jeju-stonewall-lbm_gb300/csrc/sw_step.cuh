@@ -139,23 +139,24 @@ __device__ __forceinline__ void collide(const R (&f)[Q], int x, R nu0, R cs2_18r
   const R tr = (bxx + byy + bzz) * R(1.0 / 3.0);
   const R w0 = W<R>(0), w1 = W<R>(1), w2 = W<R>(7);
   put(Int<0>{}, w0 * (r0 - R(4.5) * tr));
-  auto pair = [&](auto I, R w, R qb, R cm) {
+  // f_(+-c) = w (r0 + 4.5 Q:B) +- 3 w c.m, as two fused multiply-adds per population
+  const R wr1 = w1 * r0, wr2 = w2 * r0;
+  auto pair = [&](auto I, R w, R wr, R qb, R cm) {
     constexpr int k = decltype(I)::value;
-    const R base = w * (r0 + R(4.5) * qb);
-    const R anti = (R(3.0) * w) * cm;
-    put(Int<2 * k + 1>{}, base + anti);
-    put(Int<2 * k + 2>{}, base - anti);
+    const R base = fma(R(4.5) * w, qb, wr);
+    put(Int<2 * k + 1>{}, fma(R(3.0) * w, cm, base));
+    put(Int<2 * k + 2>{}, fma(R(-3.0) * w, cm, base));
   };
-  pair(Int<0>{}, w1, bxx - tr, mx);
-  pair(Int<1>{}, w1, byy - tr, my);
-  pair(Int<2>{}, w1, bzz - tr, mz);
+  pair(Int<0>{}, w1, wr1, bxx - tr, mx);
+  pair(Int<1>{}, w1, wr1, byy - tr, my);
+  pair(Int<2>{}, w1, wr1, bzz - tr, mz);
   const R exy = bxx + byy - tr, exz = bxx + bzz - tr, eyz = byy + bzz - tr;
-  pair(Int<3>{}, w2, exy + bxy2, mx + my);
-  pair(Int<4>{}, w2, exy - bxy2, mx - my);
-  pair(Int<5>{}, w2, exz + bxz2, mx + mz);
-  pair(Int<6>{}, w2, exz - bxz2, mx - mz);
-  pair(Int<7>{}, w2, eyz + byz2, my + mz);
-  pair(Int<8>{}, w2, eyz - byz2, my - mz);
+  pair(Int<3>{}, w2, wr2, exy + bxy2, mx + my);
+  pair(Int<4>{}, w2, wr2, exy - bxy2, mx - my);
+  pair(Int<5>{}, w2, wr2, exz + bxz2, mx + mz);
+  pair(Int<6>{}, w2, wr2, exz - bxz2, mx - mz);
+  pair(Int<7>{}, w2, wr2, eyz + byz2, my + mz);
+  pair(Int<8>{}, w2, wr2, eyz - byz2, my - mz);
   rho_out = rho;
   ux_out = ux;
   uy_out = uy;
@@ -311,6 +312,100 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(const __g
   step_segment<DT, ACC>(p, blockIdx.x, y, (int)blockIdx.z, threadIdx.x);
 }
 
+// ---------------------------------------------------------------- packed two-cell collision
+// Two cells per thread (the pair kernel) run the same collision; on sm_100+
+// the FP32 arithmetic issues as two-wide packed instructions (FFMA2 / FADD2 /
+// FMUL2 through __ffma2_rn / __fadd2_rn / __fmul2_rn), halving the issue slots
+// of the collision.  Reciprocals and square roots stay per cell.  Same
+// formulas as collide<float, true> (shifted storage).
+struct f2 {
+  float2 v;
+};
+__device__ __forceinline__ f2 F2(float a) { return {make_float2(a, a)}; }
+__device__ __forceinline__ f2 F2(float a, float b) { return {make_float2(a, b)}; }
+__device__ __forceinline__ f2 operator+(f2 a, f2 b) { return {__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ f2 operator*(f2 a, f2 b) { return {__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ f2 operator-(f2 a, f2 b) { return {__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)}; }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
+
+template <typename Put>
+__device__ __forceinline__ void collide2(const f2 (&f)[Q], int x0, float nu0, float cs2_18r2, int x_sponge,
+                                         float sponge_scale, float nu_sponge, f2 &rho_out, f2 &ux_out, f2 &uy_out,
+                                         f2 &uz_out, Put &&put) {
+  f2 s[9], d[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    s[k] = f[2 * k + 1] + f[2 * k + 2];
+    d[k] = f[2 * k + 1] - f[2 * k + 2];
+  }
+  const f2 r0 = f[0] + (((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7])) + s[8]);
+  const f2 rho = r0 + F2(1.0f);
+  const f2 mx = (d[0] + d[3]) + (d[4] + d[5]) + d[6];
+  const f2 my = (d[1] + d[3]) - d[4] + (d[7] + d[8]);
+  const f2 mz = (d[2] + d[5]) - d[6] + (d[7] - d[8]);
+  const f2 pxx = (s[0] + s[3]) + (s[4] + s[5]) + s[6];
+  const f2 pyy = (s[1] + s[3]) + (s[4] + s[7]) + s[8];
+  const f2 pzz = (s[2] + s[5]) + (s[6] + s[7]) + s[8];
+  const f2 pxy = s[3] - s[4];
+  const f2 pxz = s[5] - s[6];
+  const f2 pyz = s[7] - s[8];
+  const f2 inv = F2(rcp(rho.v.x), rcp(rho.v.y));
+  const f2 ux = mx * inv, uy = my * inv, uz = mz * inv;
+  const f2 nux = ux * F2(-1.0f), nuy = uy * F2(-1.0f), nuz = uz * F2(-1.0f);
+  const f2 third = r0 * F2(1.0f / 3.0f);
+  const f2 nxx = fma2(mx, nux, pxx - third);
+  const f2 nyy = fma2(my, nuy, pyy - third);
+  const f2 nzz = fma2(mz, nuz, pzz - third);
+  const f2 nxy = fma2(mx, nuy, pxy);
+  const f2 nxz = fma2(mx, nuz, pxz);
+  const f2 nyz = fma2(my, nuz, pyz);
+  float nua = nu0, nub = nu0;
+  if (x0 > x_sponge) {
+    const float sa = (float)(x0 - x_sponge) * sponge_scale;
+    nua = nu0 + nu_sponge * sa * sa;
+  }
+  if (x0 + 1 > x_sponge) {
+    const float sb = (float)(x0 + 1 - x_sponge) * sponge_scale;
+    nub = nu0 + nu_sponge * sb * sb;
+  }
+  const f2 tau0 = fma2(F2(3.0f), F2(nua, nub), F2(0.5f));
+  const f2 q1 = fma2(nzz, nzz, fma2(nyy, nyy, nxx * nxx));
+  const f2 q2 = fma2(nyz, nyz, fma2(nxz, nxz, nxy * nxy));
+  const f2 q = fma2(q2, F2(2.0f), q1);
+  const f2 qn = F2(fsqrt(q.v.x), fsqrt(q.v.y));
+  const f2 arg = fma2(tau0, tau0, (F2(cs2_18r2) * qn) * inv);
+  const f2 tau = F2(0.5f) * (tau0 + F2(fsqrt(arg.v.x), fsqrt(arg.v.y)));
+  const f2 keep = F2(1.0f) - F2(rcp(tau.v.x), rcp(tau.v.y));
+  const f2 bxx = fma2(keep, nxx, mx * ux), byy = fma2(keep, nyy, my * uy), bzz = fma2(keep, nzz, mz * uz);
+  const f2 bxy2 = F2(2.0f) * fma2(keep, nxy, mx * uy);
+  const f2 bxz2 = F2(2.0f) * fma2(keep, nxz, mx * uz);
+  const f2 byz2 = F2(2.0f) * fma2(keep, nyz, my * uz);
+  const f2 tr = (bxx + byy + bzz) * F2(1.0f / 3.0f);
+  const float w0 = W<float>(0), w1 = W<float>(1), w2 = W<float>(7);
+  put(Int<0>{}, F2(w0) * fma2(tr, F2(-4.5f), r0));
+  const f2 wr1 = F2(w1) * r0, wr2 = F2(w2) * r0;
+  auto pair = [&](auto I, float w, f2 wr, f2 qb, f2 cm) {
+    constexpr int k = decltype(I)::value;
+    const f2 base = fma2(F2(4.5f * w), qb, wr);
+    put(Int<2 * k + 1>{}, fma2(F2(3.0f * w), cm, base));
+    put(Int<2 * k + 2>{}, fma2(F2(-3.0f * w), cm, base));
+  };
+  pair(Int<0>{}, w1, wr1, bxx - tr, mx);
+  pair(Int<1>{}, w1, wr1, byy - tr, my);
+  pair(Int<2>{}, w1, wr1, bzz - tr, mz);
+  const f2 exy = bxx + byy - tr, exz = bxx + bzz - tr, eyz = byy + bzz - tr;
+  pair(Int<3>{}, w2, wr2, exy + bxy2, mx + my);
+  pair(Int<4>{}, w2, wr2, exy - bxy2, mx - my);
+  pair(Int<5>{}, w2, wr2, exz + bxz2, mx + mz);
+  pair(Int<6>{}, w2, wr2, exz - bxz2, mx - mz);
+  pair(Int<7>{}, w2, wr2, eyz + byz2, my + mz);
+  pair(Int<8>{}, w2, wr2, eyz - byz2, my - mz);
+  rho_out = rho;
+  ux_out = ux;
+  uy_out = uy;
+  uz_out = uz;
+}
+
 // ---------------------------------------------------------------- two cells per thread, 16-bit storage
 // One 32-bit load carries the populations of cells x0 and x0 + 1 (x0 even); a
 // warp covers 64 cells of a row.  Pulls along x take the neighbouring cell's
@@ -320,8 +415,13 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_pull(const __g
 // of their cells.
 template <int DT> struct Pack16;
 template <> struct Pack16<SW_F16_SHIFT> {
-  static __device__ __forceinline__ float lo(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v & 0xffffu))); }
-  static __device__ __forceinline__ float hi(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v >> 16))); }
+  static __device__ __forceinline__ float2 both(uint32_t v) {
+    __half2 h;
+    *reinterpret_cast<uint32_t *>(&h) = v;
+    return __half22float2(h);
+  }
+  static __device__ __forceinline__ float lo(uint32_t v) { return both(v).x; }
+  static __device__ __forceinline__ float hi(uint32_t v) { return both(v).y; }
   static __device__ __forceinline__ float one(const __half *q) { return __half2float(__ldg(q)); }
   static __device__ __forceinline__ uint32_t pack(float a, float b) {
     const __half2 h = __floats2half2_rn(a, b);
@@ -329,6 +429,9 @@ template <> struct Pack16<SW_F16_SHIFT> {
   }
 };
 template <> struct Pack16<SW_BF16_SHIFT> {
+  static __device__ __forceinline__ float2 both(uint32_t v) {
+    return make_float2(__uint_as_float(v << 16), __uint_as_float(v & 0xffff0000u));
+  }
   static __device__ __forceinline__ float lo(uint32_t v) { return __uint_as_float(v << 16); }
   static __device__ __forceinline__ float hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
   static __device__ __forceinline__ float one(const __nv_bfloat16 *q) { return __bfloat162float(__ldg(q)); }
@@ -369,67 +472,56 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
     if constexpr (ex == -1) edge[i] = (lane == 31 && live && has_r) ? PK::one(base + 2) : 0.0f;
   });
   // phase 2: pulls along x from the neighbouring lanes (outlet copies column x)
-  float a[Q], b[Q];
+  f2 v[Q];
   static_for<0, Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
     constexpr int ex = CX(i);
+    const float2 own = PK::both(P[i]);
     if constexpr (ex == 0) {
-      a[i] = PK::lo(P[i]);
-      b[i] = PK::hi(P[i]);
+      v[i].v = own;
     } else if constexpr (ex == 1) {                     // sources x0 - 1, x0
       const uint32_t prev = __shfl_up_sync(0xffffffffu, P[i], 1);
-      a[i] = lane == 0 ? edge[i] : PK::hi(prev);
-      b[i] = PK::lo(P[i]);
+      v[i] = F2(lane == 0 ? edge[i] : PK::hi(prev), own.x);
     } else {                                            // sources x0 + 1, x0 + 2
       const uint32_t next = __shfl_down_sync(0xffffffffu, P[i], 1);
       const float right = lane == 31 ? edge[i] : PK::lo(next);
-      a[i] = has_b ? PK::hi(P[i]) : PK::lo(P[i]);
-      b[i] = has_r ? right : PK::hi(P[i]);
+      v[i] = F2(has_b ? own.y : own.x, has_r ? right : own.y);
     }
   });
   if (!live) return;
   const float cs = (float)p.cs;
   const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
-  T oa[Q];
-  float ra, uxa, uya, uza;
-  collide<float, true>(a, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, ra, uxa,
-                       uya, uza, [&](auto I, float v) {
-                         constexpr int i = decltype(I)::value;
-                         oa[i] = S::from_shifted(v);
-                       });
-  if (x0 == 0) {                                        // inlet cell, lbm3d.py:67-71
-    const float u0 = __ldg(p.uin + z);
-    static_for<0, Q>([&](auto I) {
-      constexpr int i = decltype(I)::value;
-      constexpr int ex = CX(i);
-      float cu = 0.0f;
-      if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
-      cu = 3.0f * cu;
-      oa[i] = S::from_shifted(W<float>(i) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * (u0 * u0)) - W<float>(i));
-    });
-    ra = 1.0f; uxa = u0; uya = 0.0f; uza = 0.0f;
-  }
-  float rb, uxb, uyb, uzb;
-  collide<float, true>(b, x0 + 1, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rb, uxb,
-                       uyb, uzb, [&](auto I, float v) {
-                         constexpr int i = decltype(I)::value;
-                         const float va = S::to_shifted(oa[i]);
-                         if (has_b) __stcs(reinterpret_cast<unsigned int *>(out(i) + c), PK::pack(va, v));
-                         else __stcs(out(i) + c, oa[i]);
-                       });
+  const float u0 = (x0 == 0) ? __ldg(p.uin + z) : 0.0f;        // cell x0 is the inlet
+  f2 rho, ux, uy, uz;
+  collide2(v, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rho, ux, uy, uz,
+           [&](auto I, f2 o) {
+             constexpr int i = decltype(I)::value;
+             float oa = o.v.x;
+             if (x0 == 0) {                                  // lbm3d.py:67-71 for cell x0
+               constexpr int ex = CX(i);
+               float cu = 0.0f;
+               if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
+               cu = 3.0f * cu;
+               oa = W<float>(i) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * (u0 * u0)) - W<float>(i);
+             }
+             if (has_b) __stcs(reinterpret_cast<unsigned int *>(out(i) + c), PK::pack(oa, o.v.y));
+             else __stcs(out(i) + c, S::from_shifted(oa));
+           });
   if (ACC) {
-    atomicAdd(p.accp(0) + c, (double)ra);
-    atomicAdd(p.accp(1) + c, (double)uxa);
-    atomicAdd(p.accp(2) + c, (double)uya);
-    atomicAdd(p.accp(3) + c, (double)uza);
+    const bool inlet = x0 == 0;
+    atomicAdd(p.accp(0) + c, inlet ? 1.0 : (double)rho.v.x);
+    atomicAdd(p.accp(1) + c, inlet ? (double)u0 : (double)ux.v.x);
+    atomicAdd(p.accp(2) + c, inlet ? 0.0 : (double)uy.v.x);
+    atomicAdd(p.accp(3) + c, inlet ? 0.0 : (double)uz.v.x);
     if (has_b) {
-      atomicAdd(p.accp(0) + c + 1, (double)rb);
-      atomicAdd(p.accp(1) + c + 1, (double)uxb);
-      atomicAdd(p.accp(2) + c + 1, (double)uyb);
-      atomicAdd(p.accp(3) + c + 1, (double)uzb);
+      atomicAdd(p.accp(0) + c + 1, (double)rho.v.y);
+      atomicAdd(p.accp(1) + c + 1, (double)ux.v.y);
+      atomicAdd(p.accp(2) + c + 1, (double)uy.v.y);
+      atomicAdd(p.accp(3) + c + 1, (double)uz.v.y);
     }
   }
 }
+
 
 // One warp, the row segments 2 bx and 2 bx + 1 of (y, z).
 template <int DT, bool ACC, typename Ctx>
