@@ -136,6 +136,10 @@ int sw_step_accum(const sw_geom *g, int dtype, const void *f_in, void *f_out, co
 int sw_step_config_count(void);
 int sw_set_step_config(int dtype, int cfg);
 int sw_get_step_config(int dtype);
+/* The same for sw_step_accum (accumulation steps move more data per cell and
+ * may prefer another register budget). */
+int sw_set_step_config_accum(int dtype, int cfg);
+int sw_get_step_config_accum(int dtype);
 /* sw_step (acc NULL) or sw_step_accum (acc non-NULL) with an explicit configuration. */
 int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
                 const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge,

@@ -131,8 +131,9 @@ int sw_init(const sw_geom *g, int dtype, void *f, const uint8_t *flag, const flo
 }
 
 namespace {
-// launch configuration used by sw_step / sw_step_accum, per storage type
+// launch configurations used by sw_step and by sw_step_accum, per storage type
 int g_step_cfg[4] = {0, 0, 0, 0};
+int g_step_cfg_acc[4] = {0, 0, 0, 0};
 
 int step_impl(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
               const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
@@ -179,7 +180,7 @@ int sw_step_accum(const sw_geom *g, int dtype, const void *f_in, void *f_out, co
                   int64_t *force, int64_t t, double *acc, sw_stream s) {
   if (!acc) return SW_ERR_BAD_ARG;
   return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, acc,
-                   dtype_ok(dtype) ? g_step_cfg[dtype] : 0, s);
+                   dtype_ok(dtype) ? g_step_cfg_acc[dtype] : 0, s);
 }
 
 int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
@@ -198,6 +199,15 @@ int sw_set_step_config(int dtype, int cfg) {
 }
 
 int sw_get_step_config(int dtype) { return dtype_ok(dtype) ? g_step_cfg[dtype] : -1; }
+
+int sw_set_step_config_accum(int dtype, int cfg) {
+  if (!dtype_ok(dtype) || cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
+  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  g_step_cfg_acc[dtype] = cfg;
+  return SW_OK;
+}
+
+int sw_get_step_config_accum(int dtype) { return dtype_ok(dtype) ? g_step_cfg_acc[dtype] : -1; }
 
 int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !u) return SW_ERR_BAD_ARG;

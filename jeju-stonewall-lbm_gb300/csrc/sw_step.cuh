@@ -219,6 +219,13 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
   const bool top = (z == g.nz - 1);
   const int off_zm = -lev;                                          // source level of c_z = +1
   const int off_zp = top ? 0 : lev;                                 // source level of c_z = -1
+  // accumulation steps: the four running sums are read together with the
+  // populations, so their latency overlaps (each cell is owned by one thread)
+  double acc_old[4] = {0.0, 0.0, 0.0, 0.0};
+  if (ACC) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc_old[k] = __ldcs(p.accp(k) + c);
+  }
   R fl[Q];
   static_for<0, Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
@@ -258,11 +265,11 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
                           constexpr int i = decltype(I)::value;
                           S::template st<i>(out(i) + c, v);
                         });
-  if (ACC) {  // each cell is owned by one thread: reductions without a return value (no read stall)
-    atomicAdd(p.accp(0) + c, (double)rho);
-    atomicAdd(p.accp(1) + c, (double)ux);
-    atomicAdd(p.accp(2) + c, (double)uy);
-    atomicAdd(p.accp(3) + c, (double)uz);
+  if (ACC) {
+    __stcs(p.accp(0) + c, acc_old[0] + (double)rho);
+    __stcs(p.accp(1) + c, acc_old[1] + (double)ux);
+    __stcs(p.accp(2) + c, acc_old[2] + (double)uy);
+    __stcs(p.accp(3) + c, acc_old[3] + (double)uz);
   }
 }
 
@@ -471,6 +478,15 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
     if constexpr (ex == 1) edge[i] = (lane == 0 && live && x0 > 0) ? PK::one(base - 1) : 0.0f;
     if constexpr (ex == -1) edge[i] = (lane == 31 && live && has_r) ? PK::one(base + 2) : 0.0f;
   });
+  // accumulation steps: the sums of both cells, read with the populations
+  double2 acc_old[4];
+  if (ACC) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (live && has_b) acc_old[k] = __ldcs(reinterpret_cast<const double2 *>(p.accp(k) + c));
+      else acc_old[k] = make_double2(live ? __ldcs(p.accp(k) + c) : 0.0, 0.0);
+    }
+  }
   // phase 2: pulls along x from the neighbouring lanes (outlet copies column x)
   f2 v[Q];
   static_for<0, Q>([&](auto I) {
@@ -509,19 +525,22 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
            });
   if (ACC) {
     const bool inlet = x0 == 0;
-    atomicAdd(p.accp(0) + c, inlet ? 1.0 : (double)rho.v.x);
-    atomicAdd(p.accp(1) + c, inlet ? (double)u0 : (double)ux.v.x);
-    atomicAdd(p.accp(2) + c, inlet ? 0.0 : (double)uy.v.x);
-    atomicAdd(p.accp(3) + c, inlet ? 0.0 : (double)uz.v.x);
-    if (has_b) {
-      atomicAdd(p.accp(0) + c + 1, (double)rho.v.y);
-      atomicAdd(p.accp(1) + c + 1, (double)ux.v.y);
-      atomicAdd(p.accp(2) + c + 1, (double)uy.v.y);
-      atomicAdd(p.accp(3) + c + 1, (double)uz.v.y);
+    const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
+    const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
+    if (has_b) {                                        // cells x0, x0 + 1: one 16-byte update per sum
+      const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
+      __stcs(reinterpret_cast<double2 *>(p.accp(0) + c), make_double2(v0.x + ra, v0.y + (double)rho.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(1) + c), make_double2(v1.x + xa, v1.y + (double)ux.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(2) + c), make_double2(v2.x + ya, v2.y + (double)uy.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(3) + c), make_double2(v3.x + za, v3.y + (double)uz.v.y));
+    } else {
+      __stcs(p.accp(0) + c, acc_old[0].x + ra);
+      __stcs(p.accp(1) + c, acc_old[1].x + xa);
+      __stcs(p.accp(2) + c, acc_old[2].x + ya);
+      __stcs(p.accp(3) + c, acc_old[3].x + za);
     }
   }
 }
-
 
 // One warp, the row segments 2 bx and 2 bx + 1 of (y, z).
 template <int DT, bool ACC, typename Ctx>

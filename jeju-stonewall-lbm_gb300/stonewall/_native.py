@@ -87,6 +87,8 @@ def lib():
         "sw_step_config_count": ([], ctypes.c_int),
         "sw_set_step_config": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "sw_get_step_config": ([ctypes.c_int], ctypes.c_int),
+        "sw_set_step_config_accum": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "sw_get_step_config_accum": ([ctypes.c_int], ctypes.c_int),
         "sw_macro": ([G, ctypes.c_int, P, P, P, P], ctypes.c_int),
         "sw_accum": ([G, P, P, P], ctypes.c_int),
         "sw_macro_accum": ([G, ctypes.c_int, P, P, P, P, P], ctypes.c_int),

@@ -21,23 +21,25 @@ def config_count():
     return N.lib().sw_step_config_count()
 
 
-def time_configs(solver, repeats=8, warmup=2):
-    """Mean step time in ms of every configuration on the solver's grid."""
+def time_configs(solver, repeats=8, warmup=2, acc=None):
+    """Mean step time in ms of every configuration on the solver's grid (with `acc`, an Accum
+    that receives throw-away sums, the accumulating variant)."""
     L = N.lib()
     g = solver.grid
     src, dst = solver.f[solver.cur], solver.f[1 - solver.cur]
     stream = torch.cuda.current_stream()
+    accp = acc.ptr if acc is not None else None
     res = {}
     for cfg in range(config_count()):
         if L.sw_step_cfg(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
-                         solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge, None, 0, None,
+                         solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge, None, 0, accp,
                          cfg, _stream(stream)) == N.SW_ERR_UNSUPPORTED:
             continue                                  # not compiled for this storage type
 
         def launch():
             N.check(L.sw_step_cfg(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
                                   solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge,
-                                  None, 0, None, cfg, _stream(stream)), "sw_step_cfg")
+                                  None, 0, accp, cfg, _stream(stream)), "sw_step_cfg")
         for _ in range(warmup):
             launch()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -50,17 +52,26 @@ def time_configs(solver, repeats=8, warmup=2):
     return res
 
 
-def tune(solver, repeats=8, force=False):
-    """Pick and install the fastest configuration for the solver's storage type; returns (cfg, times)."""
+def tune(solver, repeats=8, force=False, accumulating=True):
+    """Pick and install the fastest configuration for the solver's storage type, for plain and for
+    accumulating steps; returns (cfg, times) of the plain steps."""
+    from .fields import Accum
     g = solver.grid
     key = (torch.cuda.get_device_name(solver.device), solver.dtype, g.nx, g.ny, g.nz)
     if key in _CACHE and not force:
-        best, times = _CACHE[key]
+        best, times, best_acc = _CACHE[key]
     else:
         times = time_configs(solver, repeats=repeats)
         best = min(times, key=times.get)
-        _CACHE[key] = (best, times)
+        best_acc = best
+        if accumulating:
+            scratch = Accum(g, device=solver.device)
+            acc_times = time_configs(solver, repeats=max(2, repeats // 2), acc=scratch)
+            best_acc = min(acc_times, key=acc_times.get)
+            del scratch
+        _CACHE[key] = (best, times, best_acc)
     N.check(N.lib().sw_set_step_config(solver.dtype, best), "sw_set_step_config")
+    N.check(N.lib().sw_set_step_config_accum(solver.dtype, best_acc), "sw_set_step_config_accum")
     return best, times
 
 
