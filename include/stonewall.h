@@ -145,6 +145,22 @@ int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, cons
                 const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge,
                 int64_t *force, int64_t t, double *acc, int cfg, sw_stream s);
 
+/* AA pattern: the same step on ONE lattice, updated in place (half the
+ * memory of f_in + f_out).  No reference counterpart: the reference always
+ * steps f0 into f1 (lbm3d.py:293-294, 362); this replaces that pair of
+ * buffers with one.  Steps alternate odd / even, starting with odd.  Before an
+ * odd step and after an even one the lattice holds the state in the usual
+ * layout (plane k holds f_k, as after sw_init or sw_pack_f), so exports,
+ * macros and checkpoints are taken after even steps; after an odd step the
+ * lattice is in transit and can only be advanced by the even step.  ghost:
+ * sw_aa_ghost_elems(g) stored values of scratch, written and read by the odd
+ * step.  acc may be NULL (otherwise as sw_step_accum).  States, forces and
+ * sums after every even step equal the two-lattice step's bit for bit. */
+int64_t sw_aa_ghost_elems(const sw_geom *g);
+int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t *flag, const uint8_t *tiles,
+               const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
+               int64_t t, double *acc, void *ghost, sw_stream s);
+
 /* k_macro, lbm3d.py:158-182 (lbm3d.py:367, 387): u = (rho, ux, uy, uz); solids -> (1, 0, 0, 0). */
 int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s);
 /* k_accum, lbm3d.py:185-188 (lbm3d.py:369): acc += u, in double. */

@@ -21,13 +21,16 @@ __device__ __forceinline__ float randf(uint32_t &st) {
   st = pcg_hash(st);
   return (float)(st >> 8) * (1.0f / 16777216.0f);
 }
+// Standard normals by Box-Muller, in float (FP64 is slow on this part; the
+// oracle's double-precision version agrees to float rounding).
 __device__ __forceinline__ float gauss_pair(uint32_t &st, float *second) {
-  double u1 = 1.0 - (double)randf(st);
-  double u2 = (double)randf(st);
-  double r = sqrt(-2.0 * log(u1));
-  double a = 6.283185307179586 * u2;
-  if (second) *second = (float)(r * sin(a));
-  return (float)(r * cos(a));
+  const float u1 = 1.0f - randf(st);  // (0, 1]
+  const float u2 = randf(st);
+  const float r = sqrtf(-2.0f * logf(u1));
+  float sn, cs;
+  sincosf(6.2831853071795865f * u2, &sn, &cs);
+  if (second) *second = r * sn;
+  return r * cs;
 }
 
 // k_init, lbm3d.py:39-54.  One thread per cell of the padded grid.

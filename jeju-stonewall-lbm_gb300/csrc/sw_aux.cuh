@@ -26,6 +26,11 @@ cudaError_t step_f32(const StepParams &p, cudaStream_t s);
 cudaError_t step_f64(const StepParams &p, cudaStream_t s);
 cudaError_t step_f16s(const StepParams &p, cudaStream_t s);
 cudaError_t step_bf16s(const StepParams &p, cudaStream_t s);
+struct AAParams;
+cudaError_t aa_f32(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s);
+cudaError_t aa_f64(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s);
+cudaError_t aa_f16s(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s);
+cudaError_t aa_bf16s(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s);
 cudaError_t batch_f32(const sw_batch_header *h, const sw_batch_entry *t, int cfg, int k, cudaStream_t s);
 cudaError_t batch_f64(const sw_batch_header *h, const sw_batch_entry *t, int cfg, int k, cudaStream_t s);
 cudaError_t batch_f16s(const sw_batch_header *h, const sw_batch_entry *t, int cfg, int k, cudaStream_t s);

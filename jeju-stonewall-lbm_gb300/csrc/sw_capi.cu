@@ -4,6 +4,7 @@
 // and returns an SW_* status; nothing here allocates or synchronises.
 #include <cstdio>
 
+#include "sw_aa.cuh"
 #include "sw_aux.cuh"
 #include "sw_batch.cuh"
 #include "sw_step.cuh"
@@ -274,6 +275,42 @@ int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_de
     case SW_F64: e = sw::batch_f64(hdr_dev, table_dev, cfg, k, st(s)); break;
     case SW_F16_SHIFT: e = sw::batch_f16s(hdr_dev, table_dev, cfg, k, st(s)); break;
     default: e = sw::batch_bf16s(hdr_dev, table_dev, cfg, k, st(s)); break;
+  }
+  return cuda_status(e);
+}
+
+int64_t sw_aa_ghost_elems(const sw_geom *g) {
+  return geom_ok(g) ? (int64_t)sw::kGhostPops * g->ny * g->nz : -1;
+}
+
+int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t *flag, const uint8_t *tiles,
+               const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
+               int64_t t, double *acc, void *ghost, sw_stream s) {
+  if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !tiles || !uin || !ghost || !aligned16(f) || t < 0)
+    return SW_ERR_BAD_ARG;
+  if (odd != 0 && odd != 1) return SW_ERR_BAD_ARG;
+  sw::StepParams p;
+  p.fin = f;
+  p.fout = f;
+  p.flag = flag;
+  p.tiles = tiles;
+  p.uin = uin;
+  p.g = to_geom(g);
+  p.nu0 = nu0;
+  p.cs = cs;
+  p.nu_sponge = nu_sponge;
+  p.x_sponge = x_sponge;
+  p.sponge_scale = (g->nx != x_sponge) ? 1.0 / (double)(g->nx - x_sponge) : 0.0;
+  p.force = force ? reinterpret_cast<long long *>(force) + (size_t)t * 2 * g->nz : nullptr;
+  p.acc = acc;
+  p.cfg = 0;
+  sw::AAParams a{ghost, ghost};
+  cudaError_t e;
+  switch (dtype) {
+    case SW_F32: e = sw::aa_f32(p, a, odd != 0, st(s)); break;
+    case SW_F64: e = sw::aa_f64(p, a, odd != 0, st(s)); break;
+    case SW_F16_SHIFT: e = sw::aa_f16s(p, a, odd != 0, st(s)); break;
+    default: e = sw::aa_bf16s(p, a, odd != 0, st(s)); break;
   }
   return cuda_status(e);
 }

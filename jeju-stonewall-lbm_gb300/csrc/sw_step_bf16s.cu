@@ -1,4 +1,5 @@
-// sw_step_bf16s.cu -- instantiations of the fused step (single lattice and batched) for SW_BF16_SHIFT.
+// sw_step_bf16s.cu -- instantiations of the fused step (single lattice, batched, AA) for SW_BF16_SHIFT.
+#include "sw_aa.cuh"
 #include "sw_aux.cuh"
 #include "sw_batch.cuh"
 #include "sw_step.cuh"
@@ -7,5 +8,8 @@ namespace sw {
 cudaError_t step_bf16s(const StepParams &p, cudaStream_t s) { return launch_step<SW_BF16_SHIFT>(p, s); }
 cudaError_t batch_bf16s(const sw_batch_header *h, const sw_batch_entry *t, int cfg, int k, cudaStream_t s) {
   return launch_batch<SW_BF16_SHIFT>(h, t, cfg, k, s);
+}
+cudaError_t aa_bf16s(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s) {
+  return launch_aa<SW_BF16_SHIFT>(p, a, odd, s);
 }
 }  // namespace sw

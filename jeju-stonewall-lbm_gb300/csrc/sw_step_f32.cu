@@ -1,4 +1,5 @@
-// sw_step_f32.cu -- instantiations of the fused step (single lattice and batched) for SW_F32.
+// sw_step_f32.cu -- instantiations of the fused step (single lattice, batched, AA) for SW_F32.
+#include "sw_aa.cuh"
 #include "sw_aux.cuh"
 #include "sw_batch.cuh"
 #include "sw_step.cuh"
@@ -7,5 +8,8 @@ namespace sw {
 cudaError_t step_f32(const StepParams &p, cudaStream_t s) { return launch_step<SW_F32>(p, s); }
 cudaError_t batch_f32(const sw_batch_header *h, const sw_batch_entry *t, int cfg, int k, cudaStream_t s) {
   return launch_batch<SW_F32>(h, t, cfg, k, s);
+}
+cudaError_t aa_f32(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s) {
+  return launch_aa<SW_F32>(p, a, odd, s);
 }
 }  // namespace sw

@@ -89,6 +89,8 @@ def lib():
         "sw_get_step_config": ([ctypes.c_int], ctypes.c_int),
         "sw_set_step_config_accum": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "sw_get_step_config_accum": ([ctypes.c_int], ctypes.c_int),
+        "sw_aa_ghost_elems": ([G], i64),
+        "sw_step_aa": ([G, ctypes.c_int, P, i32, P, P, P, f64, f64, i32, f64, P, i64, P, P, P], ctypes.c_int),
         "sw_macro": ([G, ctypes.c_int, P, P, P, P], ctypes.c_int),
         "sw_accum": ([G, P, P, P], ctypes.c_int),
         "sw_macro_accum": ([G, ctypes.c_int, P, P, P, P, P], ctypes.c_int),

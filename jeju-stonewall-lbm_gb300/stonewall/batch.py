@@ -85,6 +85,8 @@ class Batch:
     def add(self, solver):
         if solver.dtype != self.dtype:
             raise ValueError("all members of a batch share one storage type")
+        if getattr(solver, "pattern", "ab") != "ab":
+            raise ValueError("batch members use the two-lattice pattern")
         if len(self.members) >= self.max_members:
             raise RuntimeError("batch is full")
         self.members.append(solver)

@@ -93,6 +93,22 @@ def k_step(f_in: Lattice, f_out: Lattice, flag: Flags, uin, nx, ny, nz, nu0, cs,
                                       int(t), acc.ptr, _stream(stream)), "sw_step_accum")
 
 
+def k_step_aa(f: Lattice, odd, flag: Flags, uin, nu0, cs, x_sponge, nu_sponge=0.05,
+              force: ForceSeries = None, t=0, ghost=None, acc: Accum = None, stream=None):
+    """One AA-pattern step on a single lattice, in place (see include/stonewall.h, sw_step_aa)."""
+    g = _same_grid(f, flag)
+    if ghost is None or ghost.numel() < N.lib().sw_aa_ghost_elems(g.gp) * N.DTYPE_BYTES[f.dtype]:
+        raise ValueError("ghost buffer too small")
+    fptr = None
+    if force is not None:
+        if force.nz != g.nz or not (0 <= int(t) < force.n_steps):
+            raise ValueError(f"step {t} outside the force series ({force.n_steps} x {force.nz})")
+        fptr = force.ptr
+    N.check(N.lib().sw_step_aa(g.gp, f.dtype, f.ptr, int(bool(odd)), flag.ptr, flag.tiles_ptr,
+                               _uin(uin).ptr, float(nu0), float(cs), int(x_sponge), float(nu_sponge), fptr, int(t),
+                               acc.ptr if acc is not None else None, _ptr(ghost), _stream(stream)), "sw_step_aa")
+
+
 def k_macro(f: Lattice, flag: Flags, u: Macro, stream=None):
     """lbm3d.py:158-182."""
     g = _same_grid(f, flag, u)
@@ -175,5 +191,5 @@ def tables_host():
             MIRZ)
 
 
-__all__ = ["DeviceVector", "k_init", "k_step", "k_macro", "k_accum", "k_macro_accum", "launch",
+__all__ = ["DeviceVector", "k_init", "k_step", "k_step_aa", "k_macro", "k_accum", "k_macro_accum", "launch",
            "synchronize_device", "tables_host"]

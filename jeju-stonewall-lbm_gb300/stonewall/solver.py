@@ -32,8 +32,12 @@ class Diverged(RuntimeError):
 
 
 class WallSolver:
+    """pattern "ab": two lattices, each step pulls from one into the other (lbm3d.py:293-294, 362).
+    pattern "aa": one lattice updated in place (half the memory), odd and even steps alternating;
+    states, checkpoints and mean fields can be taken after an even number of steps."""
+
     def __init__(self, flag, uin, nu0, cs, x_sponge, n_total, n_spin=0, nu_sponge=0.05, dtype="f32",
-                 device="cuda", acc_every=5, chunk=50):
+                 device="cuda", acc_every=5, chunk=50, pattern="ab"):
         flag = np.asarray(flag, dtype=np.uint8)
         nx, ny, nz = flag.shape
         uin = np.asarray(uin, dtype=np.float32)
@@ -45,8 +49,20 @@ class WallSolver:
         self.uin = K.DeviceVector(uin, device=self.device)
         self.nu0, self.cs, self.x_sponge, self.nu_sponge = float(nu0), float(cs), int(x_sponge), float(nu_sponge)
         self.n_total, self.n_spin, self.acc_every = int(n_total), int(n_spin), int(acc_every)
-        self.f = [Lattice(self.grid, dtype, device=self.device),
-                  Lattice(self.grid, dtype, device=self.device).zero_()]   # f1 = zeros, lbm3d.py:294
+        if pattern not in ("ab", "aa"):
+            raise ValueError("pattern is 'ab' (two lattices) or 'aa' (one lattice, in place)")
+        self.pattern = pattern
+        if pattern == "ab":
+            self.f = [Lattice(self.grid, dtype, device=self.device),
+                      Lattice(self.grid, dtype, device=self.device).zero_()]   # f1 = zeros, lbm3d.py:294
+        else:
+            self.f = [Lattice(self.grid, dtype, device=self.device)]
+            from . import _native as N
+            nb = N.lib().sw_aa_ghost_elems(self.grid.gp) * N.DTYPE_BYTES[self.f[0].dtype]
+            self.ghost = torch.empty(int(nb), dtype=torch.uint8, device=self.device)
+            if chunk % 2:
+                raise ValueError("the AA pattern replays graphs of an even number of steps")
+        self.aa_odd_next = True      # AA: the next step is an odd one (the state is readable)
         self.cur = 0
         self.force = ForceSeries(self.n_total, nz, device=self.device)
         self.acc = Accum(self.grid, device=self.device)
@@ -60,8 +76,18 @@ class WallSolver:
     # ------------------------------------------------------------ state
     @property
     def state(self):
-        """The lattice holding the current populations (the reference's f0 after the swap)."""
-        return self.f[self.cur]
+        """The lattice holding the current populations (the reference's f0 after the swap).
+        AA pattern: the single lattice, which holds the state after an even number of steps."""
+        return self.f[self.cur] if self.pattern == "ab" else self.f[0]
+
+    def state_numpy(self, ref_dtype=np.float32):
+        """Current populations in the reference layout (19, nx, ny, nz)."""
+        self._readable()
+        return self.state.numpy(ref_dtype)
+
+    def _readable(self):
+        if self.pattern == "aa" and not self.aa_odd_next:
+            raise RuntimeError("AA pattern: the state can be read after an even number of steps only")
 
     @property
     def dtype(self):
@@ -70,7 +96,8 @@ class WallSolver:
     def memory_bytes(self):
         g = self.grid
         return (sum(f.nbytes for f in self.f) + self.flags.flag.numel() + self.flags.tiles.numel()
-                + self.force.data.numel() * 8 + self.acc.data.numel() * 8)
+                + self.force.data.numel() * 8 + self.acc.data.numel() * 8
+                + (self.ghost.numel() if self.pattern == "aa" else 0))
 
     def reload(self, flag, uin):
         """Start over with a new mask and inlet profile (torch tensors, pinned host memory copies
@@ -82,12 +109,16 @@ class WallSolver:
         self.force.data.zero_()
         self.acc.data.zero_()
         self.t, self.n_acc, self.cur = 0, 0, 0
+        self.aa_odd_next = True
         return self
 
     def autotune(self, repeats=8):
         """Time the step's launch configurations on this grid and install the fastest for this
         storage type (stonewall.autotune); the state is not modified.  Returns (cfg, times)."""
         from . import autotune
+        if self.pattern == "aa":
+            from . import _native as N
+            return N.lib().sw_get_step_config(self.dtype), {}   # the in-place step has one configuration
         return autotune.tune(self, repeats=repeats)
 
     def init(self, noise=0.02, seed=7, noise_kind="uniform"):
@@ -97,8 +128,13 @@ class WallSolver:
 
     # ------------------------------------------------------------ stepping
     def _step(self, force_rows, t_index, accumulate=False):
-        src, dst = self.f[self.cur], self.f[1 - self.cur]
         g = self.grid
+        if self.pattern == "aa":
+            K.k_step_aa(self.f[0], self.aa_odd_next, self.flags, self.uin, self.nu0, self.cs, self.x_sponge,
+                        self.nu_sponge, force_rows, t_index, ghost=self.ghost, acc=self.acc if accumulate else None)
+            self.aa_odd_next = not self.aa_odd_next
+            return
+        src, dst = self.f[self.cur], self.f[1 - self.cur]
         K.k_step(src, dst, self.flags, self.uin, g.nx, g.ny, g.nz, self.nu0, self.cs, self.x_sponge,
                  self.nu_sponge, force_rows, t_index, acc=self.acc if accumulate else None)
         self.cur ^= 1
@@ -119,11 +155,11 @@ class WallSolver:
     def _graph_for(self, key):
         if key in self._graphs:
             return self._graphs[key]
-        n, cur0, phase = key
+        n, cur0, phase = key[:3]
         if self._ring is None or self._ring.n_steps != n:
             self._ring = ForceSeries(n, self.grid.nz, device=self.device)
         ring = self._ring
-        saved_cur = self.cur
+        saved = (self.cur, self.aa_odd_next)
         self.cur = cur0
         graph = torch.cuda.CUDAGraph()
         # warm the capture path once on a side stream as torch recommends
@@ -132,7 +168,7 @@ class WallSolver:
             ring.data.zero_()
             for j in range(n):
                 self._step(ring, j, accumulate=phase is not None and (phase + j) % self.acc_every == 0)
-        self.cur = saved_cur
+        self.cur, self.aa_odd_next = saved
         n_acc = 0 if phase is None else sum(1 for j in range(n) if (phase + j) % self.acc_every == 0)
         self._graphs[key] = (graph, n_acc)
         return self._graphs[key]
@@ -144,12 +180,12 @@ class WallSolver:
         while n > 0:
             t = self.t
             same_side = t >= self.n_spin or t + c <= self.n_spin
-            if use_graphs and n >= c and same_side:
+            if use_graphs and n >= c and same_side and (self.pattern == "ab" or self.aa_odd_next):
                 phase = (t - self.n_spin) % self.acc_every if t >= self.n_spin else None
                 graph, n_acc = self._graph_for((c, self.cur, phase))
                 graph.replay()
                 self.force.data[t:t + c].copy_(self._ring.data)
-                self.cur ^= (c & 1)
+                self.cur ^= (c & 1) if self.pattern == "ab" else 0
                 self.t += c
                 self.n_acc += n_acc
                 self.launches += c
@@ -172,11 +208,14 @@ class WallSolver:
     # ------------------------------------------------------------ outputs
     def macro(self):
         """rho, ux, uy, uz of the current state in the reference layout (k_macro, lbm3d.py:367)."""
+        self._readable()
         u = Macro(self.grid, device=self.device)
         K.k_macro(self.state, self.flags, u)
         return u.numpy()
 
     def check_finite(self):
+        if self.pattern == "aa" and not self.aa_odd_next:
+            return True                 # checked at the next even boundary
         u = Macro(self.grid, device=self.device)
         K.k_macro(self.state, self.flags, u)
         if not bool(torch.isfinite(u.data).all()):
@@ -202,7 +241,7 @@ class WallSolver:
             shutil.rmtree(tmp)
         os.makedirs(tmp)
         ref_dtype = np.float64 if self.dtype == 1 else np.float32
-        np.save(os.path.join(tmp, "f.npy"), self.state.numpy(ref_dtype))
+        np.save(os.path.join(tmp, "f.npy"), self.state_numpy(ref_dtype))
         np.save(os.path.join(tmp, "force.npy"), self.force.numpy())
         np.save(os.path.join(tmp, "uacc.npy"), self.sums())
         g = self.grid
@@ -223,8 +262,10 @@ class WallSolver:
             raise ValueError(f"checkpoint {path} was made with different settings")
         self.t, self.n_acc = int(info["t"]), int(info["n_acc"])
         self.cur = 0
+        self.aa_odd_next = True
         self.f[0].assign(np.load(os.path.join(path, "f.npy")))
-        self.f[1].zero_()
+        if self.pattern == "ab":
+            self.f[1].zero_()
         self.force.assign(np.load(os.path.join(path, "force.npy")))
         self.acc.assign(np.load(os.path.join(path, "uacc.npy")))
         self._graphs.clear()

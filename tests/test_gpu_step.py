@@ -202,3 +202,17 @@ def test_every_launch_configuration_computes_the_same_step(dtype, cuda):
         dev = np.abs(outs[0][0] - W_REF[:, None, None, None])
         np.testing.assert_allclose(outs[4][0], outs[0][0], rtol=0, atol=float(4 * ulp * dev.max()))
         np.testing.assert_allclose(outs[4][1], outs[0][1], rtol=1e-3, atol=1e-6)
+
+
+def test_gaussian_init_matches_oracle(cuda, oracle_mod):
+    """Gaussian initial noise: same random stream as the oracle (float vs double Box-Muller)."""
+    from stonewall.fields import Flags, Grid, Lattice
+    from stonewall.kernels import DeviceVector, k_init
+    nx, ny, nz = 70, 13, 11
+    flag = make_mask(nx, ny, nz, 4)
+    uin = inlet(nz, 3)
+    grid = Grid(nx, ny, nz)
+    f = Lattice(grid, "f32")
+    k_init(f, Flags(grid, flag), DeviceVector(uin), 0.02, 9, "gauss")
+    want = oracle_mod.init(flag, uin, noise=np.float32(0.02), seed=9, noise_kind=1)
+    np.testing.assert_allclose(f.numpy(), want, rtol=2e-6, atol=0)
