@@ -215,6 +215,27 @@ int sw_batch_setup(int dtype, int cfg);
 int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_dev, int dtype, int cfg, int32_t k,
                   sw_stream s);
 
+/* The same batch as one CUDA graph of single-lattice launches: per entry a
+ * chain of min(k_steps, steps_left) sw_step / sw_step_accum launches (the
+ * storage type's configurations from sw_set_step_config[_accum]), the chains
+ * parallel branches between a fork and a join, so lattices run concurrently
+ * under the hardware block scheduler.  entries is a HOST table (item0 and
+ * items are not used; no sw_batch_prepare needed), at most
+ * SW_BATCH_MAX_ENTRIES long.  Each call captures the launches, updates the
+ * handle's executable graph (instantiating anew only when the number of
+ * lattices or launches changed) and launches it on s; the handle's two
+ * executable graphs alternate, so a call may wait for the launch of the call
+ * before last to finish.  One handle per device and host thread.  No
+ * reference counterpart (see sw_batch_step). */
+#define SW_BATCH_MAX_ENTRIES 256
+typedef struct sw_batch_graph sw_batch_graph;
+int sw_batch_graph_create(sw_batch_graph **out);
+int sw_batch_graph_destroy(sw_batch_graph *g);
+int sw_batch_graph_run(sw_batch_graph *g, const sw_batch_entry *entries, int32_t n, int dtype, int32_t k_steps,
+                       sw_stream s);
+/* step kernels in the graphs this handle has launched */
+int64_t sw_batch_graph_launches(const sw_batch_graph *g);
+
 /* force rows (fixed point) -> double, n values. */
 int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s);
 

@@ -47,6 +47,16 @@ __host__ __device__ inline long long batch_items(int nx, int ny, int nz, bool pa
   return (long long)nbx * ((ny + wy - 1) / wy) * nz;
 }
 
+// The accumulating variant of an item (one step in acc_every of a lattice in
+// its averaging phase) is a separate function: inlined next to the plain
+// variant its extra live values (the four float64 sums) would set the
+// register allocation of the whole loop and make the plain path spill.
+template <int DT, bool PAIR>
+__device__ __noinline__ void batch_item_acc(const BatchCtx &sc, int bx, int y, int z, int lane) {
+  if constexpr (PAIR) step_pair_segment<DT, true>(sc, bx, y, z, lane);
+  else step_segment<DT, true>(sc, bx, y, z, lane);
+}
+
 // Persistent blocks walk the items grid-stride (block b takes b, b + G, ...):
 // items that cost more (the checked path next to stones and the ground) are
 // spread over all blocks, as dynamic block scheduling would spread them.  A
@@ -121,13 +131,9 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     if (s_run) {
       const int y = yg * Cfg::WY + threadIdx.y;
       if (y < sc.g.ny) {
-        if constexpr (PAIR) {
-          if (s_acc) step_pair_segment<DT, true>(sc, bx, y, z, threadIdx.x);
-          else step_pair_segment<DT, false>(sc, bx, y, z, threadIdx.x);
-        } else {
-          if (s_acc) step_segment<DT, true>(sc, bx, y, z, threadIdx.x);
-          else step_segment<DT, false>(sc, bx, y, z, threadIdx.x);
-        }
+        if (s_acc) batch_item_acc<DT, PAIR>(sc, bx, y, z, threadIdx.x);
+        else if constexpr (PAIR) step_pair_segment<DT, false>(sc, bx, y, z, threadIdx.x);
+        else step_segment<DT, false>(sc, bx, y, z, threadIdx.x);
       }
     }
   }

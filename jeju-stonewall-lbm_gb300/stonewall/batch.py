@@ -1,13 +1,22 @@
-"""Batch: many wall solves advanced together, one persistent launch per step.
+"""Batch: many wall solves advanced together on one GPU.
 
 Each member is a WallSolver (its own buffers, mask, inlet, force series and
-sums); the batch keeps a table describing all members in device memory
-(sw_batch_entry, include/stonewall.h) and launches sw_batch_step, which walks
-every member's work in one grid of (SMs x resident blocks).  Runs of `chunk`
-steps are replayed from a CUDA graph captured once per chunk size: the kernel
-reads the table when it runs, so between replays the host only rewrites each
-member's step counter, remaining steps and current buffer (and, for serving,
-adds or drops members).  All members share one storage type.
+sums); the batch describes all members in a table (sw_batch_entry,
+include/stonewall.h).  Two modes advance the table:
+
+  "persistent": the table lives in device memory and sw_batch_step walks
+      every member's work in one launch of (SMs x resident blocks) per step.
+      Runs of `chunk` steps are replayed from a CUDA graph captured once per
+      chunk size: the kernel reads the table when it runs, so between replays
+      the host only rewrites each member's step counter, remaining steps and
+      current buffer (and, for serving, adds or drops members).
+  "graph": sw_batch_graph_run captures, per chunk, one chain of
+      single-lattice step launches per member on parallel graph branches and
+      launches the graph; the executable graph is updated in place while the
+      composition keeps its shape.
+
+autotune() times both and keeps the faster.  All members share one storage
+type.
 
 A member's results do not depend on the others (cells are owned by one
 thread, wall forces are integer sums), so a wall gives the same bits alone
@@ -45,6 +54,14 @@ def _bind():
         L.sw_batch_step.restype = ctypes.c_int
         L.sw_batch_setup.argtypes = [ctypes.c_int, ctypes.c_int]
         L.sw_batch_setup.restype = ctypes.c_int
+        L.sw_batch_graph_create.argtypes = [ctypes.POINTER(P)]
+        L.sw_batch_graph_create.restype = ctypes.c_int
+        L.sw_batch_graph_destroy.argtypes = [P]
+        L.sw_batch_graph_destroy.restype = ctypes.c_int
+        L.sw_batch_graph_run.argtypes = [P, P, ctypes.c_int32, ctypes.c_int, ctypes.c_int32, P]
+        L.sw_batch_graph_run.restype = ctypes.c_int
+        L.sw_batch_graph_launches.argtypes = [P]
+        L.sw_batch_graph_launches.restype = ctypes.c_int64
         L.sw_batch_prepare._sw_bound = True
     return L
 
@@ -59,8 +76,11 @@ def acc_steps(t0, n, n_spin, every):
     return 0 if first >= hi else (hi - 1 - first) // every + 1
 
 
+GRAPH_MAX = 256          # SW_BATCH_MAX_ENTRIES: lattices per sw_batch_graph_run
+
+
 class Batch:
-    def __init__(self, dtype="f16", device="cuda", chunk=50, max_members=512, cfg=None):
+    def __init__(self, dtype="f16", device="cuda", chunk=50, max_members=512, cfg=None, mode="persistent"):
         self.dtype = N.dtype_code(dtype)
         self.device = torch.device(device)
         self.chunk = int(chunk)
@@ -79,7 +99,26 @@ class Batch:
         self._slot = 0
         self._graphs = {}
         self.launches = 0
+        if mode not in ("persistent", "graph"):
+            raise ValueError("mode is 'persistent' or 'graph'")
+        self.mode = mode
+        self._handle = None
         _bind()
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None:
+            try:
+                N.lib().sw_batch_graph_destroy(h)
+            except Exception:
+                pass
+
+    def _graph_handle(self):
+        if self._handle is None:
+            h = ctypes.c_void_p()
+            N.check(N.lib().sw_batch_graph_create(ctypes.byref(h)), "sw_batch_graph_create")
+            self._handle = h
+        return self._handle
 
     # ------------------------------------------------------------ membership
     def add(self, solver):
@@ -99,7 +138,7 @@ class Batch:
         return [m for m in self.members if m.t < m.n_total]
 
     # ------------------------------------------------------------ table
-    def _fill(self, n_steps, tuning=False):
+    def _fill(self, n_steps, tuning=False, upload=True):
         slot = self._slot
         self._slot ^= 1
         if self._upload_done[slot] is not None:
@@ -120,7 +159,7 @@ class Batch:
             e.x_sponge, e.n_spin, e.acc_every, e.cur0 = m.x_sponge, m.n_spin, m.acc_every, m.cur
             e.t0 = m.t
             e.steps_left = min(n_steps, m.n_total - m.t)
-        if not live:
+        if not live or not upload:
             return slot, live
         N.check(N.lib().sw_batch_prepare(ctypes.byref(tab), len(live), self.dtype, self.cfg, ctypes.byref(hdr)),
                 "sw_batch_prepare")
@@ -153,21 +192,32 @@ class Batch:
             self._graphs[key] = g
         return self._graphs[key]
 
+    def _graph_run(self, slot, n_live, c):
+        if n_live > GRAPH_MAX:
+            raise RuntimeError(f"graph mode takes at most {GRAPH_MAX} lattices")
+        N.check(N.lib().sw_batch_graph_run(self._graph_handle(), ctypes.addressof(self._table_host[slot]), n_live,
+                                           self.dtype, int(c), _stream(None)), "sw_batch_graph_run")
+
     # ------------------------------------------------------------ stepping
     def advance(self, n, use_graphs=True):
         """Advance every unfinished member by up to n steps (each stops at its own n_total)."""
         n = int(n)
         while n > 0:
             c = min(self.chunk, n)
-            slot, live = self._fill(c)
+            graph_mode = self.mode == "graph"
+            slot, live = self._fill(c, upload=not graph_mode)
             if not live:
                 return self
-            if use_graphs and c == self.chunk:
+            if graph_mode:
+                self._graph_run(slot, len(live), c)
+                self.launches += sum(min(c, m.n_total - m.t) for m in live)
+            elif use_graphs and c == self.chunk:
                 self._graph(c).replay()
+                self.launches += c
             else:
                 for k in range(c):
                     self._launch(k)
-            self.launches += c
+                self.launches += c
             for m in live:
                 s = min(c, m.n_total - m.t)
                 m.n_acc += acc_steps(m.t, s, m.n_spin, m.acc_every)
@@ -185,28 +235,47 @@ class Batch:
     def cells(self):
         return sum(m.grid.cells for m in self.members)
 
-    def autotune(self, repeats=5):
-        """Time every configuration this storage type has on the current members and keep the
-        fastest.  Each timing launch recomputes every member's next state into its spare
-        buffer with forces and sums switched off, so the members' states are not changed."""
-        best, times = None, {}
-        for cfg in range(N.lib().sw_step_config_count()):
-            if not _valid(self.dtype, cfg):
-                continue
-            self.cfg = cfg
-            self._fill(1, tuning=True)
-            self._launch(0)
+    def autotune(self, repeats=5, modes=("persistent", "graph")):
+        """Time the persistent kernel in every configuration this storage type has, and the graph
+        mode (with the single-lattice configurations tuned on the largest member), on the current
+        members; keep the fastest.  Each timed step recomputes every member's next state into its
+        spare buffer with forces and sums switched off, so the members' states are not changed.
+        Returns (best, times): best is a configuration number or "graph"."""
+        times = {}
+        if "persistent" in modes:
+            for cfg in range(N.lib().sw_step_config_count()):
+                if not _valid(self.dtype, cfg):
+                    continue
+                self.cfg = cfg
+                self._fill(1, tuning=True)
+                self._launch(0)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(repeats):
+                    self._launch(0)
+                e1.record()
+                torch.cuda.synchronize()
+                times[cfg] = e0.elapsed_time(e1) / repeats
+            self.cfg = min(times, key=times.get)
+        live = self.pending()
+        if "graph" in modes and 0 < len(live) <= GRAPH_MAX:
+            from . import autotune as single
+            single.tune(max(live, key=lambda m: m.grid.cells))
+            slot, lv = self._fill(1, tuning=True, upload=False)
+            self._graph_run(slot, len(lv), 1)                       # instantiate
             torch.cuda.synchronize()
+            if hasattr(torch.cuda, "_sleep"):
+                torch.cuda._sleep(50_000_000)                       # let the host run ahead of the device
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             for _ in range(repeats):
-                self._launch(0)
+                self._graph_run(slot, len(lv), 1)
             e1.record()
             torch.cuda.synchronize()
-            times[cfg] = e0.elapsed_time(e1) / repeats
-            if best is None or times[cfg] < times[best]:
-                best = cfg
-        self.cfg = best
+            times["graph"] = e0.elapsed_time(e1) / repeats
+        best = min(times, key=times.get)
+        self.mode = "graph" if best == "graph" else "persistent"
         return best, times
 
 

@@ -6,7 +6,8 @@ Walls: for i in 0..walls-1, rng = default_rng(i) draws H from {16, 24, 32, 40}
 and porosity from U[0, 0.5]; each wall is an ellipsoid-packed stone wall with
 seed i in a 20H x 4H x 4H domain (stonewall.params.baseline_params).  All walls
 advance together in one persistent launch per step (stonewall.batch.Batch),
-replayed from a captured CUDA graph.  The plain form is the same walls solved
+replayed from a captured CUDA graph, or as one graph of per-wall launches
+per chunk (the autotuner picks the faster mode).  The plain form is the same walls solved
 one after another by WallSolver in float32.  Prints one JSON line: aggregate
 MLUPS, wall solves per hour for both forms and their ratio, and the per-wall
 relative errors of mean and peak Cd and peak Cm of the batch against the plain
@@ -62,13 +63,16 @@ def main(argv=None):
     ap.add_argument("--dtype", default="f16")
     ap.add_argument("--chunk", type=int, default=50)
     ap.add_argument("--no-plain", action="store_true", help="skip the float32 one-wall-at-a-time reference")
+    ap.add_argument("--mode", default="auto", choices=["auto", "persistent", "graph"],
+                    help="batch mode (auto: the autotuner times both)")
     a = ap.parse_args(argv)
     specs = wall_specs(a.walls)
     t_build = time.time()
     batch = Batch(dtype=a.dtype, chunk=a.chunk, max_members=max(64, a.walls))
     members = [batch.add(make_solver(sp, a.steps, a.dtype)) for sp in specs]
     t_build = time.time() - t_build
-    cfg, cfg_times = batch.autotune()
+    modes = ("persistent", "graph") if a.mode == "auto" else (a.mode,)
+    cfg, cfg_times = batch.autotune(modes=modes)
     cells = batch.cells()
     torch.cuda.synchronize()
     t0 = time.time()
@@ -80,7 +84,7 @@ def main(argv=None):
     wall_s = time.time() - t0
     gpu_ms = e0.elapsed_time(e1)
     batch_stats = [wall_stats(m) for m in members]
-    out = dict(walls=a.walls, steps=a.steps, dtype=a.dtype, cells=cells, batch_cfg=batch.cfg,
+    out = dict(walls=a.walls, steps=a.steps, dtype=a.dtype, cells=cells, batch_mode=batch.mode, batch_cfg=batch.cfg,
                batch_cfg_ms={str(k): round(v, 3) for k, v in cfg_times.items()},
                batch_seconds=round(wall_s, 3), batch_gpu_ms=round(gpu_ms, 1),
                batch_mlups=round(cells * a.steps / (gpu_ms * 1e-3) / 1e6, 1),

@@ -1,8 +1,10 @@
-"""Batched stepping: many walls in one persistent launch per step.
+"""Batched stepping: many walls in one persistent launch per step, or one graph
+of per-wall launches per chunk.
 
 A wall's results must not depend on the batch it runs in (alone vs in the mix:
 bit-identical), members with their own step counters and lengths advance
-independently, and the batched kernel computes the single-lattice step.
+independently, the batched kernel computes the single-lattice step, and the
+graph mode runs exactly the single-lattice launches.
 """
 import numpy as np
 import pytest
@@ -27,16 +29,17 @@ def _snapshot(m):
     return m.state.numpy(np.float64), m.force.data.cpu().numpy().copy(), m.sums(), m.t, m.n_acc
 
 
+@pytest.mark.parametrize("mode", ["persistent", "graph"])
 @pytest.mark.parametrize("dtype", ["f32", "f16"])
-def test_alone_equals_in_the_mix(dtype, cuda):
+def test_alone_equals_in_the_mix(dtype, mode, cuda):
     from stonewall.batch import Batch
     alone = []
     for shape, seed in SHAPES:
-        b = Batch(dtype=dtype, chunk=8)
+        b = Batch(dtype=dtype, chunk=8, mode=mode)
         m = b.add(_member(shape, seed, 40, 12, dtype))
         b.advance(40)
         alone.append(_snapshot(m))
-    mix = Batch(dtype=dtype, chunk=8)
+    mix = Batch(dtype=dtype, chunk=8, mode=mode)
     ms = [mix.add(_member(shape, seed, 40, 12, dtype)) for shape, seed in SHAPES]
     mix.advance(40)
     for a, m in zip(alone, ms):
@@ -64,10 +67,11 @@ def test_batch_matches_single_lattice_step(cuda):
         assert m.n_acc == ref.n_acc
 
 
-def test_members_with_their_own_clocks(cuda):
+@pytest.mark.parametrize("mode", ["persistent", "graph"])
+def test_members_with_their_own_clocks(mode, cuda):
     """Staggered members: one admitted late, one finishing mid-chunk; each equals its own solo run."""
     from stonewall.batch import Batch
-    b = Batch(dtype="f16", chunk=8)
+    b = Batch(dtype="f16", chunk=8, mode=mode)
     m1 = b.add(_member(SHAPES[0][0], 1, 30, 4, "f16"))
     b.advance(11)                                  # m1 at t = 11
     m2 = b.add(_member(SHAPES[1][0], 2, 13, 4, "f16"))
@@ -76,10 +80,44 @@ def test_members_with_their_own_clocks(cuda):
     b.advance(10)
     assert (m1.t, m2.t) == (30, 13) and not b.pending()
     for m, (shape, seed), n in ((m1, SHAPES[0], 30), (m2, SHAPES[1], 13)):
-        solo = Batch(dtype="f16", chunk=8)
+        solo = Batch(dtype="f16", chunk=8, mode=mode)
         r = solo.add(_member(shape, seed, n, 4, "f16"))
         solo.advance(n)
         a, c = _snapshot(m), _snapshot(r)
         for u, v in zip(a[:3], c[:3]):
             np.testing.assert_array_equal(u, v)
         assert a[3:] == c[3:]
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16"])
+def test_graph_mode_is_the_single_lattice_solve(dtype, cuda):
+    """Graph mode launches the single-lattice kernels: bit-identical to WallSolver.advance."""
+    from stonewall.batch import Batch
+    refs = []
+    for shape, seed in SHAPES:
+        r = _member(shape, seed, 37, 6, dtype)
+        r.advance(37)
+        refs.append(_snapshot(r))
+    b = Batch(dtype=dtype, chunk=10, mode="graph")
+    ms = [b.add(_member(shape, seed, 37, 6, dtype)) for shape, seed in SHAPES]
+    b.advance(37)
+    assert b.launches == 3 * 37
+    for a, m in zip(refs, ms):
+        c = _snapshot(m)
+        for u, v in zip(a[:3], c[:3]):
+            np.testing.assert_array_equal(u, v)
+        assert a[3:] == c[3:]
+
+
+def test_autotune_keeps_the_states(cuda):
+    from stonewall.batch import Batch
+    b = Batch(dtype="f16", chunk=8)
+    ms = [b.add(_member(shape, seed, 20, 4, "f16")) for shape, seed in SHAPES]
+    before = [m.state.numpy(np.float64) for m in ms]
+    best, times = b.autotune(repeats=2)
+    assert "graph" in times and best in times
+    assert b.mode == ("graph" if best == "graph" else "persistent")
+    for m, x in zip(ms, before):
+        np.testing.assert_array_equal(m.state.numpy(np.float64), x)
+    b.advance(20)
+    assert not b.pending()
