@@ -239,6 +239,19 @@ int64_t sw_batch_graph_launches(const sw_batch_graph *g);
 /* force rows (fixed point) -> double, n values. */
 int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s);
 
+/* ---------------------------------------------------------------- viewer payload
+ * From the macro field u of sw_macro (device layout [4][nz][ny][pitch]).
+ * k_slice_xz, lbm3d.py:191-194 (lbm3d.py:372): out[4][nx][nz] = u at y = y0.
+ * k_slice_xy, lbm3d.py:197-200 (lbm3d.py:373): out[4][nx][ny] = u at z = z0.
+ * k_qcoarse, lbm3d.py:203-238 (lbm3d.py:316): out[di][dj][dk] = max(0, max
+ * over the ds^3 block at (x0 + i ds, j ds, k ds) of the Q-criterion), Q taken
+ * as 0 next to non-fluid cells and outside 1 <= x < nx-1, 1 <= z < nz-1.
+ * Float32, evaluated in the reference's order without contraction. */
+int sw_slice_xz(const sw_geom *g, const float *u, int32_t y0, float *out, sw_stream s);
+int sw_slice_xy(const sw_geom *g, const float *u, int32_t z0, float *out, sw_stream s);
+int sw_qcoarse(const sw_geom *g, const float *u, const uint8_t *flag, int32_t x0, int32_t ds, int32_t di,
+               int32_t dj, int32_t dk, float *out, sw_stream s);
+
 /* ---------------------------------------------------------------- step without allocation
  * No counterpart in the reference: an addition for callers that cannot
  * allocate device memory -- a host that only receives device pointers from an

@@ -315,4 +315,79 @@ cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cuda
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- viewer payload
+// k_slice_xz / k_slice_xy (lbm3d.py:191-200): the macro field u (device layout
+// [4][nz][ny][pitch]) at y = y0 or z = z0, written in the reference layout
+// out[c][x][z] / out[c][x][y].
+__global__ void k_slice_xz(Geom g, const float *u, int y0, float *out) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 4ll * g.nx * g.nz) return;
+  const int z = (int)(k % g.nz), x = (int)((k / g.nz) % g.nx), c = (int)(k / ((long long)g.nz * g.nx));
+  out[k] = u[(size_t)c * g.plane + ((size_t)z * g.ny + y0) * g.pitch + x];
+}
+__global__ void k_slice_xy(Geom g, const float *u, int z0, float *out) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 4ll * g.nx * g.ny) return;
+  const int y = (int)(k % g.ny), x = (int)((k / g.ny) % g.nx), c = (int)(k / ((long long)g.ny * g.nx));
+  out[k] = u[(size_t)c * g.plane + ((size_t)z0 * g.ny + y) * g.pitch + x];
+}
+
+// Q-criterion at one cell (q_at, lbm3d.py:203-222): -1/2 A_ij A_ji of the
+// central-difference velocity gradient, 0 next to any non-fluid cell; y
+// periodic.  Float32 in the reference's evaluation order (this translation
+// unit is compiled without multiply-add contraction).
+__device__ float q_at(const Geom &g, const float *u, const uint8_t *flag, int x, int y, int z) {
+  const int yp = (y + 1) % g.ny, ym = (y - 1 + g.ny) % g.ny;
+  auto fl = [&](int xx, int yy, int zz) { return flag[((size_t)zz * g.ny + yy) * g.pitch + xx]; };
+  if (fl(x, y, z) != 0 || fl(x + 1, y, z) != 0 || fl(x - 1, y, z) != 0 || fl(x, yp, z) != 0 || fl(x, ym, z) != 0 ||
+      fl(x, y, z + 1) != 0 || fl(x, y, z - 1) != 0)
+    return 0.0f;
+  auto U = [&](int c, int xx, int yy, int zz) { return u[(size_t)c * g.plane + ((size_t)zz * g.ny + yy) * g.pitch + xx]; };
+  const float a11 = 0.5f * (U(1, x + 1, y, z) - U(1, x - 1, y, z));
+  const float a12 = 0.5f * (U(1, x, yp, z) - U(1, x, ym, z));
+  const float a13 = 0.5f * (U(1, x, y, z + 1) - U(1, x, y, z - 1));
+  const float a21 = 0.5f * (U(2, x + 1, y, z) - U(2, x - 1, y, z));
+  const float a22 = 0.5f * (U(2, x, yp, z) - U(2, x, ym, z));
+  const float a23 = 0.5f * (U(2, x, y, z + 1) - U(2, x, y, z - 1));
+  const float a31 = 0.5f * (U(3, x + 1, y, z) - U(3, x - 1, y, z));
+  const float a32 = 0.5f * (U(3, x, yp, z) - U(3, x, ym, z));
+  const float a33 = 0.5f * (U(3, x, y, z + 1) - U(3, x, y, z - 1));
+  return -0.5f * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0f * (a12 * a21 + a13 * a31 + a23 * a32));
+}
+
+// k_qcoarse (lbm3d.py:225-238): max of max(Q, 0) over ds^3 blocks of the crop
+// starting at (x0, 0, 0); out[i][j][k], one thread per output voxel.
+__global__ void k_qcoarse(Geom g, const float *u, const uint8_t *flag, int x0, int ds, int di, int dj, int dk,
+                          float *out) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= (long long)di * dj * dk) return;
+  const int k = (int)(n % dk), j = (int)((n / dk) % dj), i = (int)(n / ((long long)dk * dj));
+  float best = 0.0f;
+  for (int a = 0; a < ds; ++a)
+    for (int b = 0; b < ds; ++b)
+      for (int c = 0; c < ds; ++c) {
+        const int x = x0 + i * ds + a, y = j * ds + b, z = k * ds + c;
+        if (x >= 1 && x < g.nx - 1 && z >= 1 && z < g.nz - 1) best = fmaxf(best, q_at(g, u, flag, x, y, z));
+      }
+  out[n] = best;
+}
+
+cudaError_t aux_slice_xz(const Geom &g, const float *u, int y0, float *out, cudaStream_t s) {
+  const long long n = 4ll * g.nx * g.nz;
+  k_slice_xz<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, u, y0, out);
+  return cudaGetLastError();
+}
+cudaError_t aux_slice_xy(const Geom &g, const float *u, int z0, float *out, cudaStream_t s) {
+  const long long n = 4ll * g.nx * g.ny;
+  k_slice_xy<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, u, z0, out);
+  return cudaGetLastError();
+}
+cudaError_t aux_qcoarse(const Geom &g, const float *u, const uint8_t *flag, int x0, int ds, int di, int dj, int dk,
+                        float *out, cudaStream_t s) {
+  const long long n = (long long)di * dj * dk;
+  if (n == 0) return cudaSuccess;
+  k_qcoarse<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(g, u, flag, x0, ds, di, dj, dk, out);
+  return cudaGetLastError();
+}
+
 }  // namespace sw

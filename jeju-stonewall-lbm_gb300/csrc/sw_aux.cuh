@@ -18,6 +18,10 @@ cudaError_t aux_unpack_u(const Geom &g, const float *u, float *ref, cudaStream_t
 cudaError_t aux_unpack_acc(const Geom &g, const double *acc, double *ref, cudaStream_t s);
 cudaError_t aux_build_tiles(const Geom &g, const uint8_t *flag, uint8_t *tiles, cudaStream_t s);
 cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cudaStream_t s);
+cudaError_t aux_slice_xz(const Geom &g, const float *u, int y0, float *out, cudaStream_t s);
+cudaError_t aux_slice_xy(const Geom &g, const float *u, int z0, float *out, cudaStream_t s);
+cudaError_t aux_qcoarse(const Geom &g, const float *u, const uint8_t *flag, int x0, int ds, int di, int dj, int dk,
+                        float *out, cudaStream_t s);
 
 int note_cuda_error(int cuda_error);  // sw_capi.cu
 

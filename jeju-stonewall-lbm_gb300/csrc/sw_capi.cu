@@ -320,4 +320,23 @@ int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s) {
   return cuda_status(sw::aux_force_to_f64(reinterpret_cast<const long long *>(force), out, n, st(s)));
 }
 
+int sw_slice_xz(const sw_geom *g, const float *u, int32_t y0, float *out, sw_stream s) {
+  if (!geom_ok(g) || !u || !out || y0 < 0 || y0 >= g->ny) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_slice_xz(to_geom(g), u, y0, out, st(s)));
+}
+
+int sw_slice_xy(const sw_geom *g, const float *u, int32_t z0, float *out, sw_stream s) {
+  if (!geom_ok(g) || !u || !out || z0 < 0 || z0 >= g->nz) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_slice_xy(to_geom(g), u, z0, out, st(s)));
+}
+
+int sw_qcoarse(const sw_geom *g, const float *u, const uint8_t *flag, int32_t x0, int32_t ds, int32_t di,
+               int32_t dj, int32_t dk, float *out, sw_stream s) {
+  if (!geom_ok(g) || !u || !flag || !out || x0 < 0 || ds <= 0 || di < 0 || dj < 0 || dk < 0) return SW_ERR_BAD_ARG;
+  // every cell a block visits, and its +-1 neighbours in x and z, lies inside the grid
+  if ((long long)x0 + (long long)di * ds > g->nx || (long long)dj * ds > g->ny || (long long)dk * ds > g->nz)
+    return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_qcoarse(to_geom(g), u, flag, x0, ds, di, dj, dk, out, st(s)));
+}
+
 }  // extern "C"

@@ -457,6 +457,7 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
   const bool live = x0 < g.nx;        // cell x0 exists; the 32-bit pair lies inside the row
   const bool has_b = x0 + 1 < g.nx;   // cell x0 + 1 exists
   const bool has_r = x0 + 2 < g.nx;   // cell x0 + 2 exists (else the outlet copies x0 + 1)
+  const bool inlet = x0 == 0;         // cell x0 is the inlet
   const int c = (z * g.ny + y) * g.pitch + x0;
   auto in = [&](int pop) { return p.template in<T>(pop); };
   auto out = [&](int pop) { return p.template out<T>(pop); };
@@ -507,13 +508,13 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
   if (!live) return;
   const float cs = (float)p.cs;
   const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
-  const float u0 = (x0 == 0) ? __ldg(p.uin + z) : 0.0f;        // cell x0 is the inlet
+  const float u0 = inlet ? __ldg(p.uin + z) : 0.0f;
   f2 rho, ux, uy, uz;
   collide2(v, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rho, ux, uy, uz,
            [&](auto I, f2 o) {
              constexpr int i = decltype(I)::value;
              float oa = o.v.x;
-             if (x0 == 0) {                                  // lbm3d.py:67-71 for cell x0
+             if (inlet) {                                    // lbm3d.py:67-71 for cell x0
                constexpr int ex = CX(i);
                float cu = 0.0f;
                if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
@@ -524,7 +525,6 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
              else __stcs(out(i) + c, S::from_shifted(oa));
            });
   if (ACC) {
-    const bool inlet = x0 == 0;
     const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
     const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
     if (has_b) {                                        // cells x0, x0 + 1: one 16-byte update per sum

@@ -13,9 +13,11 @@ Differences, all opt-in except the last:
   --inlet clip3H|powerlaw-H  the reference's profile, or u = U0 (z/H)^(1/7) without clipping
   --noise-dist uniform|gauss
   --nz-extra                 cells added to height*H for nz (the reference adds 1)
-  Animation snapshots (snaps_xz/xy) and Q-criterion volumes (snaps_q) are
-  viewer-only outputs and are written empty; --snap-dt and --snap3d-* are
-  accepted and recorded in meta.
+  Snapshots are taken as lbm3d.py:363-377 takes them: every snap_every steps
+  after the spin-up the macro field of the state, its y = y_mid and z = z_half
+  planes (float16) and, every snap3d_every-th snapshot, a Q-criterion frame
+  max-pooled over ds^3 blocks and log-quantised to uint8 -- all on the GPU
+  (sw_slice_xz, sw_slice_xy, sw_qcoarse); they travel in the checkpoints.
 """
 import argparse
 import json
@@ -44,9 +46,10 @@ def parse(argv=None):
     ap.add_argument("--thick", type=float, default=0.3, help="wall thickness [H]")
     ap.add_argument("--t-spinup", type=float, default=20, help="spin-up time before averaging [H/U_H]")
     ap.add_argument("--t-avg", type=float, default=30, help="averaging / recording time [H/U_H]")
-    ap.add_argument("--snap-dt", type=float, default=0.25, help="snapshot interval [H/U_H] (recorded only)")
-    ap.add_argument("--snap3d-every", type=int, default=2, help="recorded only (viewer output)")
-    ap.add_argument("--snap3d-ds", type=int, default=0, help="recorded only (viewer output)")
+    ap.add_argument("--snap-dt", type=float, default=0.25, help="animation snapshot interval [H/U_H]")
+    ap.add_argument("--snap3d-every", type=int, default=2,
+                    help="save a 3D Q-criterion frame every N-th snapshot (0 = off)")
+    ap.add_argument("--snap3d-ds", type=int, default=0, help="3D frame downsampling (0 = auto, about 13 voxels per H)")
     ap.add_argument("--out", default="results", help="output directory")
     ap.add_argument("--ckpt-every", type=int, default=5000, help="checkpoint every N steps (0 = off)")
     ap.add_argument("--no-resume", action="store_true", help="ignore an existing checkpoint")
@@ -107,6 +110,11 @@ def main(argv=None):
     solver = WallSolver(flag, p.uin, p.nu0, a.Cs, p.x_sponge, p.n_total, n_spin=p.n_spin, nu_sponge=p.nu_sponge,
                         dtype=a.dtype, device=a.device, chunk=a.chunk)
     ds3 = a.snap3d_ds if a.snap3d_ds > 0 else max(1, int(round(H / 13)))
+    y_mid, z_half = ny // 2, int(round(0.5 * H)) + 1
+    q_x0 = max(1, X0 - int(round(0.5 * H)))
+    q_dims = (min(int(round(9.0 * H)), nx - 1 - q_x0) // ds3, ny // ds3, min(int(round(2.5 * H)), nz - 1) // ds3)
+    q_scale, QMAX = (H / p.UH) ** 2, 400.0
+    snaps_xz, snaps_xy, snaps_q = [], [], []
     os.makedirs(a.out, exist_ok=True)
     ckpt = os.path.join(a.out, f"{a.case}.ckpt")
     sig = dict(grid=[nx, ny, nz], H=H, porosity=a.porosity, seed=a.seed, Re=a.Re, U0=a.U0, Cs=a.Cs,
@@ -119,6 +127,9 @@ def main(argv=None):
         except ValueError:
             raise SystemExit(f"[{a.case}] checkpoint {ckpt} was made with different settings; "
                              f"use the same options, or --no-resume to start over")
+        snaps_xz = list(np.load(os.path.join(ckpt, "snaps_xz.npy")))
+        snaps_xy = list(np.load(os.path.join(ckpt, "snaps_xy.npy")))
+        snaps_q = list(np.load(os.path.join(ckpt, "snaps_q.npy")))
         print(f"[{a.case}] resumed from step {solver.t} ({solver.t/p.t_unit:.1f} H/U)", flush=True)
     else:
         solver.init(noise=0.02, seed=a.seed, noise_kind=a.noise_dist)
@@ -126,15 +137,29 @@ def main(argv=None):
     t0 = time.time()
     t_start = solver.t
     every = a.ckpt_every if a.ckpt_every > 0 else p.n_total
+    snap0 = p.n_spin + 1                       # the state after step n_spin is the first snapshot
+
+    def next_snap(t):
+        return snap0 if t < snap0 else snap0 + ((t - snap0) // p.snap_every + 1) * p.snap_every
+
     while solver.t < p.n_total:
-        nxt = min(p.n_total, (solver.t // 1000 + 1) * 1000)
+        nxt = min(p.n_total, (solver.t // 1000 + 1) * 1000, next_snap(solver.t))
         if a.ckpt_every > 0:
             nxt = min(nxt, (solver.t // every + 1) * every)
         solver.advance(nxt - solver.t)
         t = solver.t
+        k = t - snap0
+        if k >= 0 and k % p.snap_every == 0:                       # lbm3d.py:363-377
+            xz, xy = solver.snapshot(y_mid, z_half)
+            snaps_xz.append(xz)
+            snaps_xy.append(xy)
+            if a.snap3d_every > 0 and (k // p.snap_every) % a.snap3d_every == 0:
+                snaps_q.append(solver.q_frame(q_x0, ds3, q_dims, q_scale, QMAX, macro_ready=True))
         if a.ckpt_every > 0 and t % a.ckpt_every == 0 and t < p.n_total:
-            solver.save_checkpoint(ckpt, sig)
-            print(f"[{a.case}] checkpoint saved at step {t}", flush=True)
+            solver.save_checkpoint(ckpt, sig, extra=dict(
+                snaps_xz=np.array(snaps_xz), snaps_xy=np.array(snaps_xy),
+                snaps_q=np.array(snaps_q, dtype=np.uint8).reshape(-1, *q_dims)), background=True)
+            print(f"[{a.case}] checkpoint at step {t} taken (written in the background)", flush=True)
         if t % 1000 == 0 or t == p.n_total:
             torch.cuda.synchronize()
             el = time.time() - t0
@@ -151,12 +176,10 @@ def main(argv=None):
             print(f"[{a.case}] step {t}/{p.n_total}  t={t/p.t_unit:.1f} H/U  {mlups:.0f} MLUPS  "
                   f"eta {el/max(done,1)*(p.n_total-t)/60:.1f} min{chk}", flush=True)
 
+    solver.wait_checkpoint()
     fh = solver.force_series()
     co = coefficients(fh, p.UH, H, ny, p.zeta)
     mean = solver.mean_field()
-    y_mid, z_half = ny // 2, int(round(0.5 * H)) + 1
-    q_x0 = max(1, X0 - int(round(0.5 * H)))
-    q_dims = (min(int(round(9.0 * H)), nx - 1 - q_x0) // ds3, ny // ds3, min(int(round(2.5 * H)), nz - 1) // ds3)
     np.savez_compressed(
         os.path.join(a.out, f"{a.case}.npz"),
         Cd=co["Cd"].astype(np.float32), Cl=co["Cl"].astype(np.float32), Cm=co["Cm"].astype(np.float32),
@@ -165,18 +188,18 @@ def main(argv=None):
         mean_xz_spanavg=np.where(wall.any(1)[None], np.nan, mean.mean(2)).astype(np.float32),
         mean_xy_half=mean[:, :, :, z_half].astype(np.float32),
         mean3d_ds2=mean[1:, ::2, ::2, ::2].astype(np.float16),
-        snaps_xz=np.zeros((0, 3, nx, nz), np.float16), snaps_xy=np.zeros((0, 3, nx, ny), np.float16),
+        snaps_xz=np.array(snaps_xz), snaps_xy=np.array(snaps_xy),
         wall_xz=wall[:, y_mid, :], wall_xy=wall[:, :, z_half], wall_front=wall.any(0), wall_top=wall.any(2),
         wall_ds2=wall[::2, ::2, ::2],
-        snaps_q=np.zeros((0, *q_dims), np.uint8),
+        snaps_q=np.array(snaps_q, dtype=np.uint8).reshape(-1, *q_dims),
         meta=json.dumps(dict(case=a.case, porosity_target=a.porosity, porosity=float(phi), H=H, T=T, X0=X0,
-                             q3d=dict(x0=q_x0, ds=ds3, dims=list(q_dims), qmax=400.0,
+                             q3d=dict(x0=q_x0, ds=ds3, dims=list(q_dims), qmax=QMAX,
                                       every=a.snap3d_every * p.snap_every),
                              nx=nx, ny=ny, nz=nz, UH=p.UH, U0=a.U0, Re=a.Re, nu=p.nu0, Cs=a.Cs,
                              n_spin=p.n_spin, n_avg=p.n_avg, steps_per_unit=p.t_unit, snap_every=p.snap_every,
                              y_mid=y_mid, z_half=z_half, seed=a.seed, device=a.device,
                              wall_seconds=time.time() - t0, dtype=a.dtype, geom=a.geom, inlet=a.inlet,
-                             noise=a.noise_dist, snapshots="not produced (viewer output)")))
+                             noise=a.noise_dist)))
     s = slice(p.n_spin, None)
     Cd, Cm = co["Cd"][s], co["Cm"][s]
     print(f"[{a.case}] done. porosity={phi:.3f}  Cd mean={Cd.mean():.3f} max={Cd.max():.3f}  "

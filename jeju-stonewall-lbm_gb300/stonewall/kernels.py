@@ -128,6 +128,37 @@ def k_macro_accum(f: Lattice, flag: Flags, acc: Accum, u: Macro = None, stream=N
                                    _stream(stream)), "sw_macro_accum")
 
 
+def _out_f32(out, shape, what):
+    if not (isinstance(out, torch.Tensor) and out.is_cuda and out.dtype == torch.float32 and out.is_contiguous()
+            and tuple(out.shape) == tuple(shape)):
+        raise ValueError(f"{what}: out must be a contiguous float32 CUDA tensor of shape {tuple(shape)}")
+    return _ptr(out)
+
+
+def k_slice_xz(u: Macro, y0, out, stream=None):
+    """lbm3d.py:191-194: out[c, x, z] = u[c, x, y0, z] (out: float32 CUDA tensor (4, nx, nz))."""
+    g = u.grid
+    N.check(N.lib().sw_slice_xz(g.gp, u.ptr, int(y0), _out_f32(out, (4, g.nx, g.nz), "k_slice_xz"),
+                                _stream(stream)), "sw_slice_xz")
+
+
+def k_slice_xy(u: Macro, z0, out, stream=None):
+    """lbm3d.py:197-200: out[c, x, y] = u[c, x, y, z0] (out: float32 CUDA tensor (4, nx, ny))."""
+    g = u.grid
+    N.check(N.lib().sw_slice_xy(g.gp, u.ptr, int(z0), _out_f32(out, (4, g.nx, g.ny), "k_slice_xy"),
+                                _stream(stream)), "sw_slice_xy")
+
+
+def k_qcoarse(u: Macro, flag: Flags, x0, ds, nx, ny, nz, out, stream=None):
+    """lbm3d.py:225-238: Q-criterion max-pooled over ds^3 blocks from x = x0 (out: float32 CUDA tensor)."""
+    g = _same_grid(u, flag)
+    if (int(nx), int(ny), int(nz)) != (g.nx, g.ny, g.nz):
+        raise ValueError("k_qcoarse: grid extents do not match the field")
+    di, dj, dk = (int(v) for v in out.shape)
+    N.check(N.lib().sw_qcoarse(g.gp, u.ptr, flag.ptr, int(x0), int(ds), di, dj, dk,
+                               _out_f32(out, (di, dj, dk), "k_qcoarse"), _stream(stream)), "sw_qcoarse")
+
+
 def launch(kernel, dim, inputs, device=None, stream=None):
     """wp.launch-compatible entry: the reference's input lists, tables included."""
     a = list(inputs)
@@ -151,6 +182,17 @@ def launch(kernel, dim, inputs, device=None, stream=None):
     if kernel is k_accum:
         u, acc = a
         return k_accum(u, acc, stream=stream)
+    if kernel is k_slice_xz:
+        u, y0, out = a
+        return k_slice_xz(u, y0, out, stream=stream)
+    if kernel is k_slice_xy:
+        u, z0, out = a
+        return k_slice_xy(u, z0, out, stream=stream)
+    if kernel is k_qcoarse:
+        u, flag, x0, ds, nx, ny, nz, out = a
+        if tuple(int(d) for d in dim) != tuple(out.shape):
+            raise ValueError("k_qcoarse: launch dim must be the output shape")
+        return k_qcoarse(u, flag, x0, ds, nx, ny, nz, out, stream=stream)
     raise ValueError(f"unknown kernel {kernel!r}")
 
 
@@ -191,5 +233,6 @@ def tables_host():
             MIRZ)
 
 
-__all__ = ["DeviceVector", "k_init", "k_step", "k_step_aa", "k_macro", "k_accum", "k_macro_accum", "launch",
+__all__ = ["DeviceVector", "k_init", "k_step", "k_step_aa", "k_macro", "k_accum", "k_macro_accum", "k_slice_xz",
+           "k_slice_xy", "k_qcoarse", "launch",
            "synchronize_device", "tables_host"]

@@ -11,9 +11,10 @@ storage type (fp32 or fp16-shifted, by a seeded coin).  The server:
   * admits queued requests first-come first-served while their device
     footprint (both lattices, flags, sums, force series) fits under the cap;
   * keeps every admitted solve resident and advances all of them together:
-    one Batch per storage type, each replaying a captured graph of `chunk`
-    persistent launches per loop iteration, so requests that arrive while
-    others run join at the next chunk boundary;
+    one Batch per storage type advances all of its solves by `chunk` steps
+    per loop iteration (graph mode by default: one CUDA graph of per-solve
+    step chains on parallel branches; or the persistent batched kernel), so
+    requests that arrive while others run join at the next chunk boundary;
   * retires finished solves (force series -> Cd, Cm statistics), frees their
     memory and admits more.
 
@@ -99,12 +100,14 @@ def solve_stats(s):
 
 
 class Server:
-    def __init__(self, cap_bytes=160e9, chunk=50, max_members=256, device="cuda", workers=4, clock=time.monotonic):
+    def __init__(self, cap_bytes=160e9, chunk=50, max_members=256, device="cuda", workers=4, clock=time.monotonic,
+                 mode="graph"):
         self.cap = float(cap_bytes)
         self.chunk = int(chunk)
         self.device = torch.device(device)
-        self.batches = {dt: Batch(dtype=dt, chunk=chunk, max_members=max_members, device=device)
+        self.batches = {dt: Batch(dtype=dt, chunk=chunk, max_members=max_members, device=device, mode=mode)
                         for dt in ("f32", "f16")}
+        self._tuned = set()
         self.pool = cf.ThreadPoolExecutor(max_workers=workers)
         self.clock = clock
         self.resident = {}                         # rid -> (request, solver, bytes)
@@ -126,6 +129,9 @@ class Server:
             p, flag = fut.result()
             del prepared[req.rid]
             s = make_solver(req, p, flag, self.device)
+            if req.dtype not in self._tuned:             # the storage type's step configurations, once
+                s.autotune()
+                self._tuned.add(req.dtype)
             self.batches[req.dtype].add(s)
             self.resident[req.rid] = (req, s, need)
             self.used += need
@@ -198,11 +204,11 @@ class Server:
                     f16_share=round(np.mean([r.dtype == "f16" for r in done]), 3) if done else 0.0)
 
 
-def run_alone(req, device="cuda"):
+def run_alone(req, device="cuda", mode="graph"):
     """The same request solved by itself (its own batch), for alone-vs-mix checks and FP64 references."""
     p, flag = prepare(req)
     s = make_solver(req, p, flag, device)
-    b = Batch(dtype=req.dtype, chunk=50, max_members=4, device=device)
+    b = Batch(dtype=req.dtype, chunk=50, max_members=4, device=device, mode=mode)
     b.add(s)
     b.run()
     return s
@@ -220,12 +226,13 @@ def main(argv=None):
     ap.add_argument("--steps-hi", type=int, default=40000)
     ap.add_argument("--f16-share", type=float, default=0.5)
     ap.add_argument("--chunk", type=int, default=50)
+    ap.add_argument("--mode", default="graph", choices=["graph", "persistent"], help="batch mode")
     ap.add_argument("--no-drain", action="store_true", help="stop at the end of the window (unfinished solves count as not done)")
     ap.add_argument("--fp64-check", type=int, default=0, help="re-run this many completed requests in float64")
     a = ap.parse_args(argv)
     reqs = poisson_requests(a.rate, a.minutes * 60.0, seed=a.seed, H_range=(a.h_lo, a.h_hi),
                             steps=(a.steps_lo, a.steps_hi), f16_share=a.f16_share)
-    srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk)
+    srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk, mode=a.mode)
     t0 = time.monotonic()
     out = srv.serve(reqs, max_seconds=a.minutes * 60.0, drain=not a.no_drain)
     elapsed = time.monotonic() - t0

@@ -19,6 +19,7 @@ float32 files from the reference load as well.
 import json
 import os
 import shutil
+import threading
 
 import numpy as np
 import torch
@@ -72,6 +73,10 @@ class WallSolver:
         self._graphs = {}
         self._ring = None
         self.launches = 0          # kernels of this library launched by advance()
+        self._ckpt_host = None     # pinned host buffers of the checkpoint writer (reused)
+        self._ckpt_stream = None
+        self._ckpt_thread = None
+        self._ckpt_error = None
 
     # ------------------------------------------------------------ state
     @property
@@ -213,6 +218,35 @@ class WallSolver:
         K.k_macro(self.state, self.flags, u)
         return u.numpy()
 
+    def _macro_dev(self):
+        """The macro field of the current state on the device (one buffer, reused)."""
+        self._readable()
+        if getattr(self, "_u", None) is None:
+            self._u = Macro(self.grid, device=self.device)
+        K.k_macro(self.state, self.flags, self._u)
+        return self._u
+
+    def snapshot(self, y_mid, z_half):
+        """ux, uy, uz on the planes y = y_mid and z = z_half as float16 (3, nx, nz), (3, nx, ny):
+        lbm3d.py:366-375 (k_macro, k_slice_xz, k_slice_xy, [1:].astype(float16))."""
+        u = self._macro_dev()
+        g = self.grid
+        xz = torch.empty((4, g.nx, g.nz), dtype=torch.float32, device=self.device)
+        xy = torch.empty((4, g.nx, g.ny), dtype=torch.float32, device=self.device)
+        K.k_slice_xz(u, y_mid, xz)
+        K.k_slice_xy(u, z_half, xy)
+        return xz.cpu().numpy()[1:].astype(np.float16), xy.cpu().numpy()[1:].astype(np.float16)
+
+    def q_frame(self, x0, ds, dims, q_scale, qmax=400.0, macro_ready=False):
+        """Q-criterion frame of the current state: k_qcoarse then the reference's log quantisation
+        to uint8 (lbm3d.py:315-318).  macro_ready: reuse the macro field of the last snapshot()."""
+        u = self._u if macro_ready and getattr(self, "_u", None) is not None else self._macro_dev()
+        q = torch.empty(tuple(dims), dtype=torch.float32, device=self.device)
+        g = self.grid
+        K.k_qcoarse(u, self.flags, x0, ds, g.nx, g.ny, g.nz, q)
+        q = np.clip(q.cpu().numpy() * q_scale, 0, qmax)
+        return np.round(255 * np.log1p(q) / np.log1p(qmax)).astype(np.uint8)
+
     def check_finite(self):
         if self.pattern == "aa" and not self.aa_odd_next:
             return True                 # checked at the next even boundary
@@ -235,27 +269,93 @@ class WallSolver:
         return self.sums() / max(self.n_acc, 1)
 
     # ------------------------------------------------------------ checkpoints
-    def save_checkpoint(self, path, sig, extra=None):
-        tmp = path + ".tmp"
-        if os.path.isdir(tmp):
-            shutil.rmtree(tmp)
-        os.makedirs(tmp)
-        ref_dtype = np.float64 if self.dtype == 1 else np.float32
-        np.save(os.path.join(tmp, "f.npy"), self.state_numpy(ref_dtype))
-        np.save(os.path.join(tmp, "force.npy"), self.force.numpy())
-        np.save(os.path.join(tmp, "uacc.npy"), self.sums())
+    def save_checkpoint(self, path, sig, extra=None, background=False):
+        """Write the checkpoint directory (lbm3d.py:342-355).  The state, sums and force series are
+        copied on the device right away, in stream order after the steps so far; with background=True
+        the device-to-host transfer (a side stream, into reused pinned buffers) and the file writes
+        (a writer thread) overlap the steps that follow.  One checkpoint is in flight at a time;
+        wait_checkpoint() joins it and raises what it raised."""
+        self.wait_checkpoint()
+        self._readable()
         g = self.grid
-        extra = extra or {}
-        np.save(os.path.join(tmp, "snaps_xz.npy"), extra.get("snaps_xz", np.zeros((0, 3, g.nx, g.nz), np.float16)))
-        np.save(os.path.join(tmp, "snaps_xy.npy"), extra.get("snaps_xy", np.zeros((0, 3, g.nx, g.ny), np.float16)))
-        np.save(os.path.join(tmp, "snaps_q.npy"), extra.get("snaps_q", np.zeros((0, 1, 1, 1), np.uint8)))
-        with open(os.path.join(tmp, "state.json"), "w") as fh:
-            json.dump(dict(t=self.t, n_acc=self.n_acc, sig=sig), fh)
-        if os.path.isdir(path):
-            shutil.rmtree(path)
-        os.replace(tmp, path)
+        ref64 = self.dtype == 1
+        main = torch.cuda.current_stream()
+        from . import _native as N
+        from .fields import _ptr, _stream
+        f_dev = torch.empty((19, g.nx, g.ny, g.nz), dtype=torch.float64 if ref64 else torch.float32,
+                            device=self.device)
+        rd = N.SW_F64 if ref64 else N.SW_F32
+        N.check(N.lib().sw_unpack_f(g.gp, self.dtype, rd, self.state.ptr, _ptr(f_dev), _stream(main)), "sw_unpack_f")
+        acc_dev = torch.empty((4, g.nx, g.ny, g.nz), dtype=torch.float64, device=self.device)
+        N.check(N.lib().sw_unpack_acc(g.gp, self.acc.ptr, _ptr(acc_dev), _stream(main)), "sw_unpack_acc")
+        force_dev = self.force.data.clone()
+        taken = torch.cuda.Event()
+        taken.record(main)
+        host = self._ckpt_host
+        if host is None or host[0].shape != f_dev.shape or host[0].dtype != f_dev.dtype:
+            host = tuple(torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in (f_dev, acc_dev, force_dev))
+            self._ckpt_host = host
+        if self._ckpt_stream is None:
+            self._ckpt_stream = torch.cuda.Stream(device=self.device)
+        side = self._ckpt_stream
+        side.wait_event(taken)
+        with torch.cuda.stream(side):
+            for h, d in zip(host, (f_dev, acc_dev, force_dev)):
+                h.copy_(d, non_blocking=True)
+                d.record_stream(side)
+        copied = torch.cuda.Event()
+        copied.record(side)
+        solid, n_acc, state = self.flags.host != 0, self.n_acc, dict(t=self.t, n_acc=self.n_acc, sig=sig)
+        extra = dict(extra or {})
+
+        def write():
+            copied.synchronize()
+            f_h, acc_h, force_h = (h.numpy() for h in host)
+            acc_h[0][solid] = float(n_acc)                          # what k_macro + k_accum give solids
+            acc_h[1:, solid] = 0.0
+            tmp = path + ".tmp"
+            if os.path.isdir(tmp):
+                shutil.rmtree(tmp)
+            os.makedirs(tmp)
+            np.save(os.path.join(tmp, "f.npy"), f_h)
+            np.save(os.path.join(tmp, "force.npy"), force_h.astype(np.float64) / N.FORCE_SCALE)
+            np.save(os.path.join(tmp, "uacc.npy"), acc_h)
+            np.save(os.path.join(tmp, "snaps_xz.npy"),
+                    extra.get("snaps_xz", np.zeros((0, 3, g.nx, g.nz), np.float16)))
+            np.save(os.path.join(tmp, "snaps_xy.npy"),
+                    extra.get("snaps_xy", np.zeros((0, 3, g.nx, g.ny), np.float16)))
+            np.save(os.path.join(tmp, "snaps_q.npy"), extra.get("snaps_q", np.zeros((0, 1, 1, 1), np.uint8)))
+            with open(os.path.join(tmp, "state.json"), "w") as fh:
+                json.dump(state, fh)
+            if os.path.isdir(path):
+                shutil.rmtree(path)
+            os.replace(tmp, path)
+
+        if not background:
+            write()
+            return
+
+        def run():
+            try:
+                write()
+            except BaseException as e:      # handed to wait_checkpoint()
+                self._ckpt_error = e
+
+        self._ckpt_thread = threading.Thread(target=run, name="checkpoint-writer", daemon=True)
+        self._ckpt_thread.start()
+
+    def wait_checkpoint(self):
+        """Join the checkpoint being written in the background, if any."""
+        t = getattr(self, "_ckpt_thread", None)
+        if t is not None:
+            t.join()
+            self._ckpt_thread = None
+        err, self._ckpt_error = getattr(self, "_ckpt_error", None), None
+        if err is not None:
+            raise err
 
     def load_checkpoint(self, path, sig):
+        self.wait_checkpoint()
         with open(os.path.join(path, "state.json")) as fh:
             info = json.load(fh)
         if info["sig"] != sig:

@@ -112,6 +112,45 @@ def accum(u, acc):
     return acc
 
 
+def slice_xz(u, y0):
+    """k_slice_xz (lbm3d.py:191-194)."""
+    return np.ascontiguousarray(u[:, :, y0, :])
+
+
+def slice_xy(u, z0):
+    """k_slice_xy (lbm3d.py:197-200)."""
+    return np.ascontiguousarray(u[:, :, :, z0])
+
+
+def qcoarse(u, flag, x0, ds, dims):
+    """k_qcoarse with q_at (lbm3d.py:203-238) in float32 numpy, the same expression order per cell:
+    Q = -1/2 A_ij A_ji of the central-difference gradient, 0 next to non-fluid cells and outside
+    1 <= x < nx-1, 1 <= z < nz-1 (y periodic), then max(0, block max) over ds^3 blocks from x0."""
+    u = np.asarray(u, np.float32)
+    nx, ny, nz = flag.shape
+    half = np.float32(0.5)
+
+    def sh(a, dx, dy, dz):
+        return np.roll(a, -dy, axis=1)[1 + dx:nx - 1 + dx, :, 1 + dz:nz - 1 + dz]
+
+    def grad(c, dx, dy, dz):
+        return half * (sh(u[c], dx, dy, dz) - sh(u[c], -dx, -dy, -dz))
+
+    a11, a12, a13 = grad(1, 1, 0, 0), grad(1, 0, 1, 0), grad(1, 0, 0, 1)
+    a21, a22, a23 = grad(2, 1, 0, 0), grad(2, 0, 1, 0), grad(2, 0, 0, 1)
+    a31, a32, a33 = grad(3, 1, 0, 0), grad(3, 0, 1, 0), grad(3, 0, 0, 1)
+    q = -0.5 * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0 * (a12 * a21 + a13 * a31 + a23 * a32))
+    solid = flag != 0
+    near = np.zeros(q.shape, bool)
+    for d in ((0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+        near |= sh(solid, *d)
+    Q = np.zeros((nx, ny, nz), np.float32)
+    Q[1:nx - 1, :, 1:nz - 1] = np.where(near, np.float32(0.0), q)
+    di, dj, dk = dims
+    blk = Q[x0:x0 + di * ds, :dj * ds, :dk * ds].reshape(di, ds, dj, ds, dk, ds)
+    return np.maximum(np.float32(0.0), blk.max(axis=(1, 3, 5)))
+
+
 def run(f0, flag, uin, nu0, cs, x_sponge, n_steps, nu_sponge=0.05):
     """n_steps of ping-pong stepping from f0 (lbm3d.py:358-362).  Returns (f, force[n, nz, 2])."""
     fa = f0.copy()

@@ -45,6 +45,15 @@ def test_driver_matches_reference_main(tmp_path, cuda):
     np.testing.assert_allclose(a[~np.isnan(a)], b[~np.isnan(b)], rtol=1e-5, atol=1e-6)
     np.testing.assert_allclose(got["mean3d_ds2"].astype(np.float32), d["mean3d_ds2"].astype(np.float32),
                                rtol=2e-3, atol=1e-4)
+    # snapshots: float16 planes of velocities that agree to 1e-5 round to the same or an adjacent
+    # float16; Q frames are log-quantised to uint8, a level apart at most
+    for k in ("snaps_xz", "snaps_xy"):
+        assert got[k].shape == d[k].shape and got[k].dtype == np.float16, k
+        np.testing.assert_allclose(got[k].astype(np.float32), d[k].astype(np.float32), rtol=1e-3, atol=1e-6,
+                                   err_msg=k)
+    assert got["snaps_q"].shape == d["snaps_q"].shape and got["snaps_q"].dtype == np.uint8
+    assert d["snaps_q"].max() > 0
+    assert np.abs(got["snaps_q"].astype(int) - d["snaps_q"].astype(int)).max() <= 1
 
 
 def _solver(flag, uin, n_total, n_spin, chunk=8, dtype="f32"):
@@ -68,9 +77,11 @@ def test_graph_replay_equals_eager(cuda):
     assert a.n_acc == b.n_acc == len(range(13, 60, 5))
 
 
+@pytest.mark.parametrize("background", [False, True])
 @pytest.mark.parametrize("dtype", ["f32", "f16"])
-def test_resume_is_bit_identical(tmp_path, cuda, dtype):
-    """Checkpoint at step 25, resume in a new solver, finish: same forces, sums and state."""
+def test_resume_is_bit_identical(tmp_path, cuda, dtype, background):
+    """Checkpoint at step 25, resume in a new solver, finish: same forces, sums and state.  With
+    background=True the writing overlaps 20 more steps of the solver that took it."""
     from gpu_helpers import inlet, make_mask
     flag = make_mask(40, 12, 14, 10)
     uin = inlet(14, 4)
@@ -79,7 +90,10 @@ def test_resume_is_bit_identical(tmp_path, cuda, dtype):
     part = _solver(flag, uin, 50, 10, dtype=dtype)
     part.advance(25)
     ck = str(tmp_path / "c.ckpt")
-    part.save_checkpoint(ck, dict(a=1))
+    part.save_checkpoint(ck, dict(a=1), background=background)
+    if background:
+        part.advance(20)                           # overwrites the state the checkpoint was taken from
+        part.wait_checkpoint()
     res = _solver(flag, uin, 50, 10, dtype=dtype)
     info = res.load_checkpoint(ck, dict(a=1))
     assert info["t"] == 25

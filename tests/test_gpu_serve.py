@@ -30,13 +30,14 @@ def test_server_completes_everything_under_the_cap(cuda):
     assert summ["completed"] == len(reqs) and summ["p99_latency_s"] >= summ["p50_latency_s"]
 
 
-def test_result_is_the_same_alone_and_in_the_mix(cuda):
+@pytest.mark.parametrize("mode", ["graph", "persistent"])
+def test_result_is_the_same_alone_and_in_the_mix(mode, cuda):
     from stonewall.serve import Server, run_alone, solve_stats
     reqs = _requests()
-    srv = Server(cap_bytes=1e12, chunk=16)
+    srv = Server(cap_bytes=1e12, chunk=16, mode=mode)
     out = srv.serve(reqs)
     for r in out[:4]:
-        alone = run_alone(r)
+        alone = run_alone(r, mode=mode)
         st = solve_stats(alone)
         for k, v in st.items():
             assert v == r.result["stats"][k] or (np.isnan(v) and np.isnan(r.result["stats"][k])), (r.rid, k)
