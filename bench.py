@@ -287,7 +287,8 @@ def run_ours(a):
     roofline = dict(bound="hbm", achieved=round(achieved, 1), peak=peak, unit="GB/s", frac=round(achieved / peak, 4),
                     traffic=traffic, peak_source=f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind ==
                     "measured" else "fallback 6.8 TB/s",
-                    kernel="k_step_pull", step_ms=round(step_ms, 4), alg_bytes_per_launch=alg_bytes,
+                    kernel="k_step_pull" if cfg < 4 else ("k_step_pair" if cfg < 8 else "k_step_tma"),
+                    step_ms=round(step_ms, 4), alg_bytes_per_launch=alg_bytes,
                     bytes_per_fluid_cell=BYTES_PER_CELL[dtype])
     del solver
     torch.cuda.empty_cache()

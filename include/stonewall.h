@@ -129,11 +129,17 @@ int sw_step_accum(const sw_geom *g, int dtype, const void *f_in, void *f_out, co
                   double nu_sponge, int64_t *force, int64_t t, double *acc, sw_stream s);
 
 /* Launch configurations of the step (block shape and register budget, see
- * csrc/sw_step.cuh).  sw_step and sw_step_accum use the configuration set for
- * their storage type (process-wide, default 0); stonewall/autotune.py times
- * every configuration with sw_step_cfg and sets the fastest.  No reference
- * counterpart (Warp chooses its own launch shape). */
+ * csrc/sw_step.cuh): 0-3 one cell per thread, 4-7 two cells per thread and
+ * 8-10 two cells per thread with TMA-staged sources (csrc/sw_tma.cuh), the
+ * last two groups for 16-bit storage only.  sw_step and sw_step_accum use the
+ * configuration set for their storage type (process-wide, default 0);
+ * stonewall/autotune.py times every configuration with sw_step_cfg and sets
+ * the fastest.  No reference counterpart (Warp chooses its own launch shape). */
 int sw_step_config_count(void);
+/* Blocks of the TMA-staged configurations that gave up a bounded wait for
+ * their copies since the last call (read and cleared; -1 if unreadable).  A
+ * non-zero count means the steps they belonged to are not valid. */
+int64_t sw_tma_timeouts(void);
 int sw_set_step_config(int dtype, int cfg);
 int sw_get_step_config(int dtype);
 /* The same for sw_step_accum (accumulation steps move more data per cell and

@@ -24,6 +24,8 @@ cudaError_t aux_qcoarse(const Geom &g, const float *u, const uint8_t *flag, int 
                         float *out, cudaStream_t s);
 
 int note_cuda_error(int cuda_error);  // sw_capi.cu
+unsigned int tma_timeouts_f16s();      // read and clear the TMA wait time-outs of sw_step_f16s.cu
+unsigned int tma_timeouts_bf16s();
 
 // one launcher per storage type, each in its own translation unit (sw_step_<dtype>.cu)
 cudaError_t step_f32(const StepParams &p, cudaStream_t s);

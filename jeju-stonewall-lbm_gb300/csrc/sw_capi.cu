@@ -192,6 +192,12 @@ int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, cons
 
 int sw_step_config_count(void) { return sw::kStepConfigs; }
 
+int64_t sw_tma_timeouts(void) {
+  const unsigned a = sw::tma_timeouts_f16s(), b = sw::tma_timeouts_bf16s();
+  if (a == ~0u || b == ~0u) return -1;
+  return (int64_t)a + (int64_t)b;
+}
+
 int sw_set_step_config(int dtype, int cfg) {
   if (!dtype_ok(dtype) || cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
   if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
@@ -229,10 +235,10 @@ int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *fl
 int sw_batch_prepare(sw_batch_entry *entries, int32_t n, int dtype, int cfg, sw_batch_header *hdr) {
   if (!entries || n <= 0 || !hdr || !dtype_ok(dtype)) return SW_ERR_BAD_ARG;
   if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
-  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  if (!sw::batch_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
   int wy = 0;
   bool pair = false;
-  sw::config_shape(cfg, &wy, &pair);
+  if (!sw::config_shape(cfg, &wy, &pair)) return SW_ERR_UNSUPPORTED;
   long long item0 = 0;
   for (int i = 0; i < n; ++i) {
     sw_batch_entry &e = entries[i];
@@ -253,7 +259,7 @@ int sw_batch_prepare(sw_batch_entry *entries, int32_t n, int dtype, int cfg, sw_
 
 int sw_batch_setup(int dtype, int cfg) {
   if (!dtype_ok(dtype) || cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
-  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  if (!sw::batch_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
   cudaError_t e;
   switch (dtype) {
     case SW_F32: e = sw::batch_f32(nullptr, nullptr, cfg, -1, nullptr); break;
@@ -268,7 +274,7 @@ int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_de
                   sw_stream s) {
   if (!hdr_dev || !table_dev || !dtype_ok(dtype) || k < 0) return SW_ERR_BAD_ARG;
   if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
-  if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  if (!sw::batch_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
   cudaError_t e;
   switch (dtype) {
     case SW_F32: e = sw::batch_f32(hdr_dev, table_dev, cfg, k, st(s)); break;

@@ -175,7 +175,10 @@ template <int WY_, int MINB_> struct StepCfg {
 #define SW_STEP_CONFIGS(X) X(0, 8, 4) X(1, 8, 5) X(2, 4, 8) X(3, 4, 12)
 // two cells per thread (16-bit storage only), see k_step_pair
 #define SW_PAIR_CONFIGS(X) X(4, 4, 8) X(5, 4, 10) X(6, 8, 4) X(7, 8, 5)
-constexpr int kStepConfigs = 8;
+// two cells per thread with TMA-staged sources (16-bit storage only), see sw_tma.cuh:
+// (id, row-groups per block, stages, resident blocks)
+#define SW_TMA_CONFIGS(X) X(8, 4, 2, 8) X(9, 8, 3, 6) X(10, 4, 2, 10)
+constexpr int kStepConfigs = 11;
 
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
 // tests (segments next to stones, the ground or a fluid cell at z = 0).
@@ -591,7 +594,13 @@ cudaError_t launch_pair(const StepParams &p, cudaStream_t s) {
 constexpr bool is16(int dt) { return dt == SW_F16_SHIFT || dt == SW_BF16_SHIFT; }
 
 // Whether configuration cfg exists for storage type dt.
-inline bool step_config_valid(int dt, int cfg) { return (cfg >= 0 && cfg < 4) || (cfg >= 4 && cfg < 8 && is16(dt)); }
+inline bool step_config_valid(int dt, int cfg) { return (cfg >= 0 && cfg < 4) || (cfg >= 4 && cfg < 11 && is16(dt)); }
+// Whether the persistent batched kernel has configuration cfg (not the TMA-staged ones).
+inline bool batch_config_valid(int dt, int cfg) { return cfg < 8 && step_config_valid(dt, cfg); }
+
+}  // namespace sw
+#include "sw_tma.cuh"
+namespace sw {
 
 template <int DT>
 cudaError_t launch_step(const StepParams &p_in, cudaStream_t s) {
@@ -612,6 +621,15 @@ cudaError_t launch_step(const StepParams &p_in, cudaStream_t s) {
     else                                                                                           \
       return cudaErrorNotSupported;
     SW_PAIR_CONFIGS(SW_CASE)
+#undef SW_CASE
+#define SW_CASE(ID, ITEMS, NSTAGE, MINB)                                                          \
+  case ID:                                                                                         \
+    if constexpr (is16(DT))                                                                        \
+      return p.acc ? launch_tma<DT, true, TmaCfg<ITEMS, NSTAGE, MINB>>(p, s)                      \
+                   : launch_tma<DT, false, TmaCfg<ITEMS, NSTAGE, MINB>>(p, s);                    \
+    else                                                                                           \
+      return cudaErrorNotSupported;
+    SW_TMA_CONFIGS(SW_CASE)
 #undef SW_CASE
     default:
       return cudaErrorInvalidValue;

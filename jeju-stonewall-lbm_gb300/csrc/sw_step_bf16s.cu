@@ -12,4 +12,5 @@ cudaError_t batch_bf16s(const sw_batch_header *h, const sw_batch_entry *t, int c
 cudaError_t aa_bf16s(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s) {
   return launch_aa<SW_BF16_SHIFT>(p, a, odd, s);
 }
+unsigned int tma_timeouts_bf16s() { return tma_timeouts_take(); }
 }  // namespace sw

@@ -12,4 +12,5 @@ cudaError_t batch_f16s(const sw_batch_header *h, const sw_batch_entry *t, int cf
 cudaError_t aa_f16s(const StepParams &p, const AAParams &a, bool odd, cudaStream_t s) {
   return launch_aa<SW_F16_SHIFT>(p, a, odd, s);
 }
+unsigned int tma_timeouts_f16s() { return tma_timeouts_take(); }
 }  // namespace sw

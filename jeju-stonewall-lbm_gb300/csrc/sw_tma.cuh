@@ -1,0 +1,310 @@
+// sw_tma.cuh -- the 16-bit step with its pull sources staged in shared memory by TMA.
+//
+// Included by sw_step.cuh after the cell code it reuses (collide2, Pack16,
+// step_cell, warp_force_add).  Same cells, same arithmetic, same results as
+// the two-cells-per-thread kernel (k_step_pair); what changes is how the 19
+// pulled values reach the registers.  k_step_pair loads every population row
+// with 32-bit loads and moves the x-shifted ones between lanes (shuffles plus
+// per-lane edge loads), which costs more issue slots than the collision
+// itself; here one thread per block describes, per population, the whole
+// source tile of the block -- an 80-cell x WY-row box of one population plane
+// at level z - c_z (the mirrored plane at the top), x from x0 - 8 -- to the
+// tensor-memory accelerator, which copies it into shared memory and signals an
+// mbarrier.  Warps then read their two cells' sources from the box row at the
+// shifted offset (two aligned 32-bit shared loads and a byte permute for
+// c_x = +-1, one load otherwise).
+//
+// Boxes start on 16-byte boundaries (x0 - 8 is a multiple of 8 halves); a box
+// reaching outside the lattice reads zeros there: x < 0 only feeds the inlet
+// cell (which does not pull), x >= nx only the outlet copy (handled by the
+// same per-lane selects as k_step_pair), z < 0 only ground rows (never on the
+// fast path).  The periodic y wrap is not a box: the warp whose source row
+// is -1 or ny reads a one-row box of row ny - 1 or 0 loaded beside the stage.
+//
+// A block runs ITEMS consecutive y row-groups of one 64-cell x segment pair at
+// one level, with NSTAGE stages in flight.  Every wait on an mbarrier is
+// bounded; on time-out the block records the event in g_tma_timeouts, waits
+// (bounded) for its copies in flight and leaves.
+#pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+namespace sw {
+
+template <int ITEMS_, int NSTAGE_, int MINB_> struct TmaCfg {
+  static constexpr int WY = 4;
+  static constexpr int THREADS = 32 * WY;
+  static constexpr int ITEMS = ITEMS_;
+  static constexpr int NSTAGE = NSTAGE_;
+  static constexpr int MINB = MINB_;
+};
+
+constexpr int kTmaBoxX = 80;                                 // halves per box row: 8 + 64 + 8
+constexpr int kTmaRowBytes = kTmaBoxX * 2;                   // 160
+constexpr int kTmaBoxBytes = kTmaRowBytes * 4;               // one population, WY = 4 rows: 640 (5 x 128)
+constexpr int kTmaWrapBytes = 256;                           // one-row box (160 B) in a 128-aligned slot
+constexpr int kTmaWrapSlots = 10;                            // the populations with c_y != 0
+constexpr int kTmaStageBytes = Q * kTmaBoxBytes + kTmaWrapSlots * kTmaWrapBytes;
+
+// wrap slot of a population with c_y != 0 (3, 4, 7, 8, 9, 10, 15, 16, 17, 18)
+__host__ __device__ constexpr int wrap_slot(int i) {
+  return i == 3 ? 0 : i == 4 ? 1 : i == 7 ? 2 : i == 8 ? 3 : i == 9 ? 4 : i == 10 ? 5 : i == 15 ? 6 : i == 16 ? 7
+       : i == 17 ? 8 : i == 18 ? 9 : -1;
+}
+
+// blocks that gave up waiting (must stay 0); one counter per translation unit
+static __device__ unsigned int g_tma_timeouts;
+
+// Reads and clears this translation unit's time-out counter (host).
+static inline unsigned int tma_timeouts_take() {
+  unsigned int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tma_timeouts, sizeof(v)) != cudaSuccess) return ~0u;
+  if (v != 0 && cudaMemcpyToSymbol(g_tma_timeouts, &zero, sizeof(zero)) != cudaSuccess) return ~0u;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait: about 2^20 polls (each try_wait itself suspends for a while), then false.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int k = 0; k < (1 << 20); ++k) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (k > 64) __nanosleep(64);
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+
+
+// Issue the copies of item (x0, y0, z) into stage `st`, arriving on `bar` (one thread).
+__device__ __forceinline__ void tma_issue(const CUtensorMap *map, const CUtensorMap *map1, const Geom &g, int x0,
+                                          int y0, int z, uint32_t st, uint32_t bar) {
+  const bool top = z == g.nz - 1;
+  const bool wrap_lo = y0 == 0;                  // source row -1 of the first warp (c_y = +1)
+  const bool wrap_hi = y0 + 4 >= g.ny;           // source row ny of the warp at y = ny - 1 (c_y = -1)
+  uint32_t bytes = Q * kTmaBoxBytes;
+  if (wrap_lo) bytes += 5 * kTmaRowBytes;
+  if (wrap_hi) bytes += 5 * kTmaRowBytes;
+  mbar_expect_tx(bar, bytes);
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ey = CY(i), ez = CZ(i);
+    const int pop = (ez == -1 && top) ? MIRZ(i) : i;
+    const int zl = (ez == -1 && top) ? z : z - ez;
+    tma_load_4d(st + i * kTmaBoxBytes, map, x0 - 8, y0 - ey, zl, pop, bar);
+    if constexpr (ey == 1) {
+      if (wrap_lo) tma_load_4d(st + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes, map1, x0 - 8, g.ny - 1, zl, pop, bar);
+    } else if constexpr (ey == -1) {
+      if (wrap_hi) tma_load_4d(st + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes, map1, x0 - 8, 0, zl, pop, bar);
+    }
+  });
+}
+
+// The pair-kernel fast path with the sources read from the staged boxes (st: the stage).
+template <int DT, bool ACC>
+__device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t *st, int x0, int y, int z, int w,
+                                              int lane) {
+  using S = Store<DT>;
+  using PK = Pack16<DT>;
+  const Geom &g = p.g;
+  const bool live = x0 < g.nx;
+  const bool has_b = x0 + 1 < g.nx;
+  const bool has_r = x0 + 2 < g.nx;
+  const bool inlet = x0 == 0;
+  const int c = (z * g.ny + y) * g.pitch + x0;
+  const int lane_word = 4 + lane;                                     // 32-bit word of elements 8 + 2 lane, + 1
+  f2 v[Q];
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = CX(i), ey = CY(i);
+    const uint8_t *rowp = st + i * kTmaBoxBytes + w * kTmaRowBytes;
+    if constexpr (ey == 1) {
+      if (y == 0) rowp = st + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes;
+    } else if constexpr (ey == -1) {
+      if (y == g.ny - 1) rowp = st + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes;
+    }
+    const uint32_t *row = reinterpret_cast<const uint32_t *>(rowp);
+    const uint32_t own = row[lane_word];                               // cells x0, x0 + 1
+    if constexpr (ex == 0) {
+      v[i].v = PK::both(own);
+    } else if constexpr (ex == 1) {                                   // sources x0 - 1, x0
+      const uint32_t left = row[lane_word - 1];
+      v[i] = F2(PK::hi(left), PK::lo(own));
+    } else {                                                          // sources x0 + 1, x0 + 2 (outlet: x)
+      const uint32_t right = row[lane_word + 1];
+      const float2 o = PK::both(own);
+      v[i] = F2(has_b ? o.y : o.x, has_r ? PK::lo(right) : o.y);
+    }
+  });
+  double2 acc_old[4];
+  if (ACC && live) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (has_b) acc_old[k] = __ldcs(reinterpret_cast<const double2 *>(p.accp(k) + c));
+      else acc_old[k] = make_double2(__ldcs(p.accp(k) + c), 0.0);
+    }
+  }
+  if (!live) return;
+  const float cs = (float)p.cs;
+  const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
+  const float u0 = inlet ? __ldg(p.uin + z) : 0.0f;
+  f2 rho, ux, uy, uz;
+  collide2(v, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rho, ux, uy, uz,
+           [&](auto I, f2 o) {
+             constexpr int i = decltype(I)::value;
+             float oa = o.v.x;
+             if (inlet) {                                             // lbm3d.py:67-71 for cell x0
+               constexpr int ex = CX(i);
+               float cu = 0.0f;
+               if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
+               cu = 3.0f * cu;
+               oa = W<float>(i) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * (u0 * u0)) - W<float>(i);
+             }
+             typename S::T *out = p.template out<typename S::T>(i) + c;
+             if (has_b) __stcs(reinterpret_cast<unsigned int *>(out), PK::pack(oa, o.v.y));
+             else __stcs(out, S::from_shifted(oa));
+           });
+  if (ACC) {
+    const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
+    const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
+    if (has_b) {
+      const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
+      __stcs(reinterpret_cast<double2 *>(p.accp(0) + c), make_double2(v0.x + ra, v0.y + (double)rho.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(1) + c), make_double2(v1.x + xa, v1.y + (double)ux.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(2) + c), make_double2(v2.x + ya, v2.y + (double)uy.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(3) + c), make_double2(v3.x + za, v3.y + (double)uz.v.y));
+    } else {
+      __stcs(p.accp(0) + c, acc_old[0].x + ra);
+      __stcs(p.accp(1) + c, acc_old[1].x + xa);
+      __stcs(p.accp(2) + c, acc_old[2].x + ya);
+      __stcs(p.accp(3) + c, acc_old[3].x + za);
+    }
+  }
+}
+
+// Grid: (ceil(pitch / 64), ceil(ceil(ny / 4) / ITEMS), nz); block = 4 warps, warp w = row y0 + w.
+template <int DT, bool ACC, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
+    k_step_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap map1,
+               const __grid_constant__ StepParams p) {
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  __shared__ __align__(8) unsigned long long bars[Cfg::NSTAGE];
+  uint8_t *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);   // 128-byte aligned boxes
+  const Geom &g = p.g;
+  const int w = threadIdx.y, lane = threadIdx.x;
+  const bool leader = w == 0 && lane == 0;
+  const int bx = blockIdx.x, z = blockIdx.z;
+  const int x0s = 2 * SEG * bx;                                        // first cell of the segment pair
+  const int nyb = (g.ny + 3) / 4;
+  const int yb0 = blockIdx.y * Cfg::ITEMS;
+  const int n_items = min(Cfg::ITEMS, nyb - yb0);
+  const uint32_t base = smem_u32(smem);
+  if (leader) {
+    for (int s = 0; s < Cfg::NSTAGE; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    for (int j = 0; j < Cfg::NSTAGE && j < n_items; ++j)
+      tma_issue(&map, &map1, g, x0s, (yb0 + j) * 4, z, base + j * kTmaStageBytes, smem_u32(&bars[j]));
+  }
+  __syncthreads();
+  bool ok = true;
+  int j = 0;
+  for (; j < n_items; ++j) {
+    const int s = j % Cfg::NSTAGE;
+    const uint32_t st = base + s * kTmaStageBytes;
+    const int y = (yb0 + j) * 4 + w;
+    if (ok) ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((j / Cfg::NSTAGE) & 1));
+    if (ok && y < g.ny) {
+      const int seg = (z * g.ny + y) * g.nseg_x + 2 * bx;
+      const bool has_tb = 2 * bx + 1 < g.nseg_x;
+      const uint8_t ka = __ldg(p.tiles + seg);
+      const uint8_t kb = has_tb ? __ldg(p.tiles + seg + 1) : (uint8_t)TILE_ALL_SOLID;
+      if (!(ka & kb & TILE_ALL_SOLID)) {
+        const int x0 = x0s + 2 * lane;
+        if (!((ka | kb) & TILE_CHECK)) {
+          tma_pair_fast<DT, ACC>(p, smem + s * kTmaStageBytes, x0, y, z, w, lane);
+        } else {                                                      // next to stones / ground: per cell
+          float fxw = 0.0f, fzw = 0.0f;
+          int hit = 0;
+          if (x0 < g.nx) step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
+          if (x0 + 1 < g.nx) step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
+          if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+        }
+      }
+    }
+    ok = __syncthreads_and(ok);                                       // stage s is free again
+    if (!ok) break;
+    if (leader && j + Cfg::NSTAGE < n_items)
+      tma_issue(&map, &map1, g, x0s, (yb0 + j + Cfg::NSTAGE) * 4, z, st, smem_u32(&bars[s]));
+  }
+  if (!ok && leader) {                                                // item j failed: items j .. j+NSTAGE-1
+    atomicAdd(&g_tma_timeouts, 1u);                                   // were issued; let their copies land
+    for (int k = j; k < n_items && k < j + Cfg::NSTAGE; ++k)
+      (void)mbar_wait(smem_u32(&bars[k % Cfg::NSTAGE]), (uint32_t)((k / Cfg::NSTAGE) & 1));
+  }
+}
+
+// ---------------------------------------------------------------- host side
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// The lattice f (16-bit elements, [19][nz][ny][pitch]) as a 4-D tensor, boxes of 80 x rows x 1 x 1.
+inline bool encode_lattice_map(CUtensorMap *m, const void *f, const Geom &g, int rows) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dim[4] = {(cuuint64_t)g.pitch, (cuuint64_t)g.ny, (cuuint64_t)g.nz, (cuuint64_t)Q};
+  const cuuint64_t stride[3] = {(cuuint64_t)g.pitch * 2, (cuuint64_t)g.pitch * g.ny * 2, (cuuint64_t)g.plane * 2};
+  const cuuint32_t box[4] = {(cuuint32_t)kTmaBoxX, (cuuint32_t)rows, 1, 1};
+  const cuuint32_t estride[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<void *>(f), dim, stride, box, estride,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int DT, bool ACC, typename Cfg>
+cudaError_t launch_tma(const StepParams &p, cudaStream_t s) {
+  CUtensorMap map, map1;
+  if (!encode_lattice_map(&map, p.fin, p.g, 4) || !encode_lattice_map(&map1, p.fin, p.g, 1))
+    return cudaErrorNotSupported;
+  const int smem = Cfg::NSTAGE * kTmaStageBytes + 128;               // + alignment slack; <= 48 KB
+  static_assert(Cfg::NSTAGE * kTmaStageBytes + 128 <= 48 * 1024, "stages exceed the default shared memory");
+  const int nyb = (p.g.ny + 3) / 4;
+  const dim3 grid((unsigned)((p.g.nseg_x + 1) / 2), (unsigned)((nyb + Cfg::ITEMS - 1) / Cfg::ITEMS), (unsigned)p.g.nz);
+  k_step_tma<DT, ACC, Cfg><<<grid, dim3(32, 4), smem, s>>>(map, map1, p);
+  return cudaGetLastError();
+}
+
+}  // namespace sw

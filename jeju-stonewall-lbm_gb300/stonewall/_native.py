@@ -95,6 +95,7 @@ def lib():
         "sw_accum": ([G, P, P, P], ctypes.c_int),
         "sw_macro_accum": ([G, ctypes.c_int, P, P, P, P, P], ctypes.c_int),
         "sw_force_to_f64": ([P, P, i64, P], ctypes.c_int),
+        "sw_tma_timeouts": ([], i64),
         "sw_slice_xz": ([G, P, i32, P, P], ctypes.c_int),
         "sw_slice_xy": ([G, P, i32, P, P], ctypes.c_int),
         "sw_qcoarse": ([G, P, P, i32, i32, i32, i32, i32, P, P], ctypes.c_int),

@@ -280,4 +280,5 @@ class Batch:
 
 
 def _valid(dtype, cfg):
-    return cfg < 4 or dtype in (N.SW_F16_SHIFT, N.SW_BF16_SHIFT)
+    """Configurations of the persistent batched kernel (the TMA-staged ones, 8 and up, are not)."""
+    return cfg < 4 or (cfg < 8 and dtype in (N.SW_F16_SHIFT, N.SW_BF16_SHIFT))
