@@ -165,6 +165,7 @@ int step_impl(const sw_geom *g, int dtype, const void *f_in, void *f_out, const 
     case SW_F16_SHIFT: e = sw::step_f16s(p, st(s)); break;
     default: e = sw::step_bf16s(p, st(s)); break;
   }
+  if (e == cudaErrorNotSupported) return SW_ERR_UNSUPPORTED;   // e.g. no tensor-map encoder in the driver
   return cuda_status(e);
 }
 }  // namespace

@@ -451,10 +451,61 @@ template <> struct Pack16<SW_BF16_SHIFT> {
   }
 };
 
+// Collision of a cell pair and its stores.  Both cells of the pair are stored
+// with one 32-bit store even when cell x0 + 1 lies past the row end: that
+// half lands in the row's padding columns (x >= nx), which nothing reads.  The
+// inlet cell (x0 == 0, lbm3d.py:67-71) is collided like the others and then
+// overwritten by its equilibrium in a branch only its lane takes.
 template <int DT, bool ACC, typename Ctx>
-__device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int z, int lane) {
+__device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q], int x0, int c, int z, bool inlet,
+                                                   const double2 (&acc_old)[4]) {
   using S = Store<DT>;
   using T = typename S::T;
+  using PK = Pack16<DT>;
+  const float cs = (float)p.cs;
+  const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
+  f2 rho, ux, uy, uz;
+  collide2(v, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rho, ux, uy, uz,
+           [&](auto I, f2 o) {
+             constexpr int i = decltype(I)::value;
+             __stcs(reinterpret_cast<unsigned int *>(p.template out<T>(i) + c), PK::pack(o.v.x, o.v.y));
+           });
+  float u0 = 0.0f;
+  if (inlet) {
+    u0 = __ldg(p.uin + z);
+    const float usq = u0 * u0;
+    static_for<0, Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      constexpr int ex = CX(i);
+      float cu = 0.0f;
+      if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
+      cu = 3.0f * cu;
+      const float w = W<float>(i) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * usq);
+      __stcs(p.template out<T>(i) + c, S::from_shifted(w - W<float>(i)));
+    });
+  }
+  if (ACC) {
+    const bool has_b = x0 + 1 < p.g.nx;
+    const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
+    const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
+    if (has_b) {                                        // cells x0, x0 + 1: one 16-byte update per sum
+      const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
+      __stcs(reinterpret_cast<double2 *>(p.accp(0) + c), make_double2(v0.x + ra, v0.y + (double)rho.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(1) + c), make_double2(v1.x + xa, v1.y + (double)ux.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(2) + c), make_double2(v2.x + ya, v2.y + (double)uy.v.y));
+      __stcs(reinterpret_cast<double2 *>(p.accp(3) + c), make_double2(v3.x + za, v3.y + (double)uz.v.y));
+    } else {
+      __stcs(p.accp(0) + c, acc_old[0].x + ra);
+      __stcs(p.accp(1) + c, acc_old[1].x + xa);
+      __stcs(p.accp(2) + c, acc_old[2].x + ya);
+      __stcs(p.accp(3) + c, acc_old[3].x + za);
+    }
+  }
+}
+
+template <int DT, bool ACC, typename Ctx>
+__device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int z, int lane) {
+  using T = typename Store<DT>::T;
   using PK = Pack16<DT>;
   const Geom &g = p.g;
   const bool live = x0 < g.nx;        // cell x0 exists; the 32-bit pair lies inside the row
@@ -463,7 +514,6 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
   const bool inlet = x0 == 0;         // cell x0 is the inlet
   const int c = (z * g.ny + y) * g.pitch + x0;
   auto in = [&](int pop) { return p.template in<T>(pop); };
-  auto out = [&](int pop) { return p.template out<T>(pop); };
   const int row = g.pitch, lev = g.ny * g.pitch;
   const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
   const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
@@ -509,40 +559,7 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
     }
   });
   if (!live) return;
-  const float cs = (float)p.cs;
-  const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
-  const float u0 = inlet ? __ldg(p.uin + z) : 0.0f;
-  f2 rho, ux, uy, uz;
-  collide2(v, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rho, ux, uy, uz,
-           [&](auto I, f2 o) {
-             constexpr int i = decltype(I)::value;
-             float oa = o.v.x;
-             if (inlet) {                                    // lbm3d.py:67-71 for cell x0
-               constexpr int ex = CX(i);
-               float cu = 0.0f;
-               if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
-               cu = 3.0f * cu;
-               oa = W<float>(i) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * (u0 * u0)) - W<float>(i);
-             }
-             if (has_b) __stcs(reinterpret_cast<unsigned int *>(out(i) + c), PK::pack(oa, o.v.y));
-             else __stcs(out(i) + c, S::from_shifted(oa));
-           });
-  if (ACC) {
-    const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
-    const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
-    if (has_b) {                                        // cells x0, x0 + 1: one 16-byte update per sum
-      const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
-      __stcs(reinterpret_cast<double2 *>(p.accp(0) + c), make_double2(v0.x + ra, v0.y + (double)rho.v.y));
-      __stcs(reinterpret_cast<double2 *>(p.accp(1) + c), make_double2(v1.x + xa, v1.y + (double)ux.v.y));
-      __stcs(reinterpret_cast<double2 *>(p.accp(2) + c), make_double2(v2.x + ya, v2.y + (double)uy.v.y));
-      __stcs(reinterpret_cast<double2 *>(p.accp(3) + c), make_double2(v3.x + za, v3.y + (double)uz.v.y));
-    } else {
-      __stcs(p.accp(0) + c, acc_old[0].x + ra);
-      __stcs(p.accp(1) + c, acc_old[1].x + xa);
-      __stcs(p.accp(2) + c, acc_old[2].x + ya);
-      __stcs(p.accp(3) + c, acc_old[3].x + za);
-    }
-  }
+  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, acc_old);
 }
 
 // One warp, the row segments 2 bx and 2 bx + 1 of (y, z).

@@ -82,9 +82,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return done != 0;
 }
-// Bounded wait: about 2^20 polls (each try_wait itself suspends for a while), then false.
+// Bounded wait: 2^14 polls with back-off (a copy lands in microseconds; this gives up
+// after milliseconds), then false.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int k = 0; k < (1 << 20); ++k) {
+  for (int k = 0; k < (1 << 14); ++k) {
     if (mbar_try_wait(bar, parity)) return true;
     if (k > 64) __nanosleep(64);
   }
@@ -128,7 +129,6 @@ __device__ __forceinline__ void tma_issue(const CUtensorMap *map, const CUtensor
 template <int DT, bool ACC>
 __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t *st, int x0, int y, int z, int w,
                                               int lane) {
-  using S = Store<DT>;
   using PK = Pack16<DT>;
   const Geom &g = p.g;
   const bool live = x0 < g.nx;
@@ -169,41 +169,7 @@ __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t
     }
   }
   if (!live) return;
-  const float cs = (float)p.cs;
-  const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
-  const float u0 = inlet ? __ldg(p.uin + z) : 0.0f;
-  f2 rho, ux, uy, uz;
-  collide2(v, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rho, ux, uy, uz,
-           [&](auto I, f2 o) {
-             constexpr int i = decltype(I)::value;
-             float oa = o.v.x;
-             if (inlet) {                                             // lbm3d.py:67-71 for cell x0
-               constexpr int ex = CX(i);
-               float cu = 0.0f;
-               if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
-               cu = 3.0f * cu;
-               oa = W<float>(i) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * (u0 * u0)) - W<float>(i);
-             }
-             typename S::T *out = p.template out<typename S::T>(i) + c;
-             if (has_b) __stcs(reinterpret_cast<unsigned int *>(out), PK::pack(oa, o.v.y));
-             else __stcs(out, S::from_shifted(oa));
-           });
-  if (ACC) {
-    const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
-    const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
-    if (has_b) {
-      const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
-      __stcs(reinterpret_cast<double2 *>(p.accp(0) + c), make_double2(v0.x + ra, v0.y + (double)rho.v.y));
-      __stcs(reinterpret_cast<double2 *>(p.accp(1) + c), make_double2(v1.x + xa, v1.y + (double)ux.v.y));
-      __stcs(reinterpret_cast<double2 *>(p.accp(2) + c), make_double2(v2.x + ya, v2.y + (double)uy.v.y));
-      __stcs(reinterpret_cast<double2 *>(p.accp(3) + c), make_double2(v3.x + za, v3.y + (double)uz.v.y));
-    } else {
-      __stcs(p.accp(0) + c, acc_old[0].x + ra);
-      __stcs(p.accp(1) + c, acc_old[1].x + xa);
-      __stcs(p.accp(2) + c, acc_old[2].x + ya);
-      __stcs(p.accp(3) + c, acc_old[3].x + za);
-    }
-  }
+  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, acc_old);
 }
 
 // Grid: (ceil(pitch / 64), ceil(ceil(ny / 4) / ITEMS), nz); block = 4 warps, warp w = row y0 + w.

@@ -9,7 +9,9 @@ storage type (fp32 or fp16-shifted, by a seeded coin).  The server:
 
   * builds masks on host threads while requests wait (CPU work off the loop);
   * admits queued requests first-come first-served while their device
-    footprint (both lattices, flags, sums, force series) fits under the cap;
+    footprint (both lattices, flags, sums, force series) fits under the cap
+    and the resident cells stay under --max-cells (beyond what saturates the
+    GPU more residents only stretch every solve's time to result);
   * keeps every admitted solve resident and advances all of them together:
     one Batch per storage type advances all of its solves by `chunk` steps
     per loop iteration (graph mode by default: one CUDA graph of per-solve
@@ -21,6 +23,10 @@ storage type (fp32 or fp16-shifted, by a seeded coin).  The server:
 Reported: p50 / p99 time-to-result (arrival to result), queueing and run
 times, solves per hour over the run, GPU throughput.  A solve's result does
 not depend on what it shared the GPU with (see stonewall.batch).
+
+--plain serves the same stream the plain way for comparison: one request at a
+time, first come first served, float32 storage whatever the request asked
+for, one WallSolver per request (graph-replayed steps, no batching).
 """
 import argparse
 import concurrent.futures as cf
@@ -78,6 +84,11 @@ def footprint(req):
             + p.nz * 4)
 
 
+def cells_of(req):
+    p = baseline_params(req.H, req.steps, UH=req.U)
+    return p.nx * p.ny * p.nz
+
+
 def prepare(req):
     """Host side of a request: parameters and the flag array (run on a worker thread)."""
     p = baseline_params(req.H, req.steps, UH=req.U)
@@ -101,8 +112,10 @@ def solve_stats(s):
 
 class Server:
     def __init__(self, cap_bytes=160e9, chunk=50, max_members=256, device="cuda", workers=4, clock=time.monotonic,
-                 mode="graph"):
+                 mode="graph", max_cells=None):
         self.cap = float(cap_bytes)
+        self.max_cells = float(max_cells) if max_cells else float("inf")
+        self.cells = 0
         self.chunk = int(chunk)
         self.device = torch.device(device)
         self.batches = {dt: Batch(dtype=dt, chunk=chunk, max_members=max_members, device=device, mode=mode)
@@ -125,6 +138,8 @@ class Server:
                 raise ValueError(f"request {req.rid} needs {need/1e9:.1f} GB, more than the cap")
             if self.used + need > self.cap:
                 return
+            if self.resident and self.cells + cells_of(req) > self.max_cells:
+                return
             queue.pop(0)
             p, flag = fut.result()
             del prepared[req.rid]
@@ -135,6 +150,7 @@ class Server:
             self.batches[req.dtype].add(s)
             self.resident[req.rid] = (req, s, need)
             self.used += need
+            self.cells += s.grid.cells
             req.t_admit = now
 
     def _retire(self, now):
@@ -146,6 +162,7 @@ class Server:
                               run=now - req.t_admit, cells=s.grid.cells)
             self.batches[req.dtype].remove(s)
             self.used -= need
+            self.cells -= s.grid.cells
             del s
         return len(done)
 
@@ -204,6 +221,56 @@ class Server:
                     f16_share=round(np.mean([r.dtype == "f16" for r in done]), 3) if done else 0.0)
 
 
+class PlainServer:
+    """The plain form: one request at a time, first come first served, float32, no batching."""
+
+    def __init__(self, chunk=50, device="cuda", workers=4, clock=time.monotonic):
+        self.chunk, self.device, self.clock = int(chunk), torch.device(device), clock
+        self.pool = cf.ThreadPoolExecutor(max_workers=workers)
+        self.log, self.max_used = [], 0.0
+
+    def serve(self, requests, max_seconds=None, drain=True, log_every=30.0):
+        reqs = sorted(requests, key=lambda r: r.t_arrive)
+        queue, prepared = [], {}
+        t0 = self.clock()
+        i, tuned = 0, False
+        while True:
+            now = self.clock() - t0
+            while i < len(reqs) and reqs[i].t_arrive <= now:
+                queue.append(reqs[i])
+                prepared[reqs[i].rid] = self.pool.submit(prepare, reqs[i])
+                i += 1
+            if max_seconds is not None and now > max_seconds and not drain:
+                break
+            if not queue:
+                if i >= len(reqs):
+                    break
+                time.sleep(0.005)
+                continue
+            req = queue.pop(0)
+            p, flag = prepared.pop(req.rid).result()
+            req.t_admit = self.clock() - t0
+            s = WallSolver(flag, p.uin, p.nu0, p.Cs, p.x_sponge, req.steps, n_spin=p.n_spin, dtype="f32",
+                           device=self.device, chunk=self.chunk)
+            s.init(noise=0.02, seed=req.seed, noise_kind="gauss")
+            s.params = p
+            if not tuned:
+                s.autotune()
+                tuned = True
+            s.advance(req.steps)
+            st = solve_stats(s)
+            now = self.clock() - t0
+            req.result = dict(stats=st, t_done=now, latency=now - req.t_arrive, wait=req.t_admit - req.t_arrive,
+                              run=now - req.t_admit, cells=s.grid.cells)
+            self.max_used = max(self.max_used, s.memory_bytes())
+            del s
+            if max_seconds is not None and now > max_seconds and drain and i < len(reqs):
+                reqs = reqs[:i]
+        self.pool.shutdown(wait=False)
+        self.unfinished = dict(queued=len(queue), resident=0)
+        return reqs
+
+
 def run_alone(req, device="cuda", mode="graph"):
     """The same request solved by itself (its own batch), for alone-vs-mix checks and FP64 references."""
     p, flag = prepare(req)
@@ -227,18 +294,24 @@ def main(argv=None):
     ap.add_argument("--f16-share", type=float, default=0.5)
     ap.add_argument("--chunk", type=int, default=50)
     ap.add_argument("--mode", default="graph", choices=["graph", "persistent"], help="batch mode")
+    ap.add_argument("--max-cells", type=float, default=1.2e8, help="resident cells admitted at most (0 = no limit)")
+    ap.add_argument("--plain", action="store_true", help="serve the plain way (one float32 solve at a time)")
     ap.add_argument("--no-drain", action="store_true", help="stop at the end of the window (unfinished solves count as not done)")
     ap.add_argument("--fp64-check", type=int, default=0, help="re-run this many completed requests in float64")
     a = ap.parse_args(argv)
     reqs = poisson_requests(a.rate, a.minutes * 60.0, seed=a.seed, H_range=(a.h_lo, a.h_hi),
                             steps=(a.steps_lo, a.steps_hi), f16_share=a.f16_share)
-    srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk, mode=a.mode)
+    if a.plain:
+        srv = PlainServer(chunk=a.chunk)
+    else:
+        srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk, mode=a.mode, max_cells=a.max_cells or None)
     t0 = time.monotonic()
     out = srv.serve(reqs, max_seconds=a.minutes * 60.0, drain=not a.no_drain)
     elapsed = time.monotonic() - t0
     summ = srv.summary(out, elapsed)
-    summ.update(unfinished_at_end=srv.unfinished, max_resident_gb=round(srv.max_used / 1e9, 2), cap_gb=a.cap_gb,
-                arrivals_per_s=a.rate, window_minutes=a.minutes)
+    summ.update(form="plain" if a.plain else f"batched ({a.mode})", unfinished_at_end=srv.unfinished,
+                max_resident_gb=round(srv.max_used / 1e9, 2), cap_gb=a.cap_gb, arrivals_per_s=a.rate,
+                window_minutes=a.minutes, seed=a.seed, drained=not a.no_drain)
     if a.fp64_check:
         done = sorted([r for r in out if r.result is not None], key=lambda r: r.H * r.steps)[:a.fp64_check]
         errs = []

@@ -41,3 +41,33 @@ def test_result_is_the_same_alone_and_in_the_mix(mode, cuda):
         st = solve_stats(alone)
         for k, v in st.items():
             assert v == r.result["stats"][k] or (np.isnan(v) and np.isnan(r.result["stats"][k])), (r.rid, k)
+
+
+def test_plain_form_serves_the_same_stream(cuda):
+    """The comparison form: one float32 solve at a time, first come first served."""
+    from stonewall.serve import PlainServer, Server
+    reqs = _requests()
+    out = PlainServer(chunk=16).serve(reqs)
+    assert all(r.result is not None for r in out)
+    done = sorted(out, key=lambda r: r.result["t_done"])
+    assert [r.rid for r in done] == [r.rid for r in sorted(out, key=lambda r: r.t_arrive)]
+    assert all(r.result["wait"] >= 0 for r in out)
+    summ = Server.summary(out, 10.0)
+    assert summ["completed"] == len(reqs)
+
+
+def test_resident_cells_cap_limits_concurrency(cuda):
+    from stonewall.serve import Server, cells_of
+    reqs = _requests()
+    cap_cells = 1.5 * max(cells_of(r) for r in reqs)
+    srv = Server(cap_bytes=1e12, chunk=16, max_cells=cap_cells)
+    seen = []
+    orig = srv._admit
+
+    def spy(queue, prepared, now):
+        orig(queue, prepared, now)
+        seen.append(srv.cells)
+    srv._admit = spy
+    out = srv.serve(reqs)
+    assert all(r.result is not None for r in out)
+    assert max(seen) <= cap_cells

@@ -71,3 +71,35 @@ def test_oracle_thread_count_invariance(oracle_mod):
     oracle_mod.set_threads(nmax)
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+def test_oracle_qcoarse_equals_the_per_cell_loop():
+    """The vectorised k_qcoarse restatement against a per-cell loop over q_at (lbm3d.py:203-238)."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(5)
+    nx, ny, nz = 12, 5, 7
+    u = rng.normal(0, 0.05, (4, nx, ny, nz)).astype(np.float32)
+    flag = (rng.random((nx, ny, nz)) < 0.1).astype(np.uint8)
+    h = np.float32(0.5)
+
+    def q_at(x, y, z):
+        yp, ym = (y + 1) % ny, (y - 1 + ny) % ny
+        if (flag[x, y, z] or flag[x + 1, y, z] or flag[x - 1, y, z] or flag[x, yp, z] or flag[x, ym, z]
+                or flag[x, y, z + 1] or flag[x, y, z - 1]):
+            return np.float32(0.0)
+        g = [[h * (u[c, x + 1, y, z] - u[c, x - 1, y, z]), h * (u[c, x, yp, z] - u[c, x, ym, z]),
+              h * (u[c, x, y, z + 1] - u[c, x, y, z - 1])] for c in (1, 2, 3)]
+        return np.float32(-0.5) * (g[0][0] * g[0][0] + g[1][1] * g[1][1] + g[2][2] * g[2][2]
+                                   + np.float32(2.0) * (g[0][1] * g[1][0] + g[0][2] * g[2][0] + g[1][2] * g[2][1]))
+
+    for x0, ds in ((1, 1), (2, 2)):
+        dims = ((nx - 1 - x0) // ds, ny // ds, (nz - 1) // ds)
+        want = np.zeros(dims, np.float32)
+        for i, j, k in np.ndindex(*dims):
+            best = np.float32(0.0)
+            for a, b, c in np.ndindex(ds, ds, ds):
+                x, y, z = x0 + i * ds + a, j * ds + b, k * ds + c
+                if 1 <= x < nx - 1 and 1 <= z < nz - 1:
+                    best = max(best, q_at(x, y, z))
+            want[i, j, k] = best
+        np.testing.assert_array_equal(O.qcoarse(u, flag, x0, ds, dims), want)
