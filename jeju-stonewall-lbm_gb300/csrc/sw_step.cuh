@@ -177,7 +177,7 @@ template <int WY_, int MINB_> struct StepCfg {
 #define SW_PAIR_CONFIGS(X) X(4, 4, 8) X(5, 4, 10) X(6, 8, 4) X(7, 8, 5)
 // two cells per thread with TMA-staged sources (16-bit storage only), see sw_tma.cuh:
 // (id, row-groups per block, stages, resident blocks)
-#define SW_TMA_CONFIGS(X) X(8, 4, 2, 8) X(9, 8, 3, 6) X(10, 4, 2, 10)
+#define SW_TMA_CONFIGS(X) X(8, 4, 2, 8) X(9, 2, 2, 8) X(10, 4, 2, 10)
 constexpr int kStepConfigs = 11;
 
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
@@ -611,7 +611,9 @@ cudaError_t launch_pair(const StepParams &p, cudaStream_t s) {
 constexpr bool is16(int dt) { return dt == SW_F16_SHIFT || dt == SW_BF16_SHIFT; }
 
 // Whether configuration cfg exists for storage type dt.
-inline bool step_config_valid(int dt, int cfg) { return (cfg >= 0 && cfg < 4) || (cfg >= 4 && cfg < 11 && is16(dt)); }
+inline bool step_config_valid(int dt, int cfg) {
+  return (cfg >= 0 && cfg < 4) || (cfg >= 4 && cfg < kStepConfigs && is16(dt));
+}
 // Whether the persistent batched kernel has configuration cfg (not the TMA-staged ones).
 inline bool batch_config_valid(int dt, int cfg) { return cfg < 8 && step_config_valid(dt, cfg); }
 

@@ -22,7 +22,9 @@
 // is -1 or ny reads a one-row box of row ny - 1 or 0 loaded beside the stage.
 //
 // A block runs ITEMS consecutive y row-groups of one 64-cell x segment pair at
-// one level, with NSTAGE stages in flight.  Every wait on an mbarrier is
+// one level, with NSTAGE stages in flight (measured at c2: 4 row-groups and 2
+// stages beat 1, 2, 8 and 16 row-groups, 3 stages, and a variant with a
+// producer warp releasing stages through mbarriers instead of a block barrier).  Every wait on an mbarrier is
 // bounded; on time-out the block records the event in g_tma_timeouts, waits
 // (bounded) for its copies in flight and leaves.
 #pragma once
