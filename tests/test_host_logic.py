@@ -1,0 +1,53 @@
+"""Host-side logic that needs no GPU: accumulation schedules, request streams and footprints,
+batch table layout, graph-batch argument checks."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def test_acc_steps_counts_the_accumulating_steps():
+    from stonewall.batch import acc_steps
+    for t0 in range(0, 40, 3):
+        for n in range(0, 25, 4):
+            for n_spin in (0, 7, 30):
+                for every in (1, 5):
+                    want = sum(1 for t in range(t0, t0 + n) if t >= n_spin and (t - n_spin) % every == 0)
+                    assert acc_steps(t0, n, n_spin, every) == want, (t0, n, n_spin, every)
+
+
+def test_batch_entry_matches_the_c_layout():
+    """sw_batch_entry in include/stonewall.h: 144 bytes, the fields at their C offsets."""
+    from stonewall.batch import SwBatchEntry, SwBatchHeader
+    assert ctypes.sizeof(SwBatchEntry) == 144
+    assert ctypes.sizeof(SwBatchHeader) == 16
+    off = {name: getattr(SwBatchEntry, name).offset for name, _ in SwBatchEntry._fields_}
+    assert off["geom"] == 0 and off["item0"] == 16 and off["f"] == 32 and off["nu0"] == 88
+    assert off["x_sponge"] == 112 and off["t0"] == 128 and off["steps_left"] == 136
+
+
+def test_poisson_requests_are_seeded_and_in_range():
+    from stonewall.serve import cells_of, footprint, poisson_requests
+    a = poisson_requests(2.0, 60.0, seed=3)
+    b = poisson_requests(2.0, 60.0, seed=3)
+    assert [(r.t_arrive, r.H, r.steps, r.dtype) for r in a] == [(r.t_arrive, r.H, r.steps, r.dtype) for r in b]
+    assert 60 < len(a) < 200                                   # about rate x duration
+    t = np.array([r.t_arrive for r in a])
+    assert (np.diff(t) > 0).all() and t[-1] < 60.0
+    for r in a:
+        assert 16 <= r.H <= 48 and 5000 <= r.steps <= 40000 and 0.03 <= r.U <= 0.06 and 0 <= r.porosity <= 0.5
+        assert r.dtype in ("f32", "f16")
+        cells = cells_of(r)
+        per_cell = 2 * 19 * (4 if r.dtype == "f32" else 2) + 33
+        assert footprint(r) >= per_cell * cells
+
+
+def test_graph_batch_rejects_bad_arguments(native_lib):
+    from stonewall import _native as N
+    from stonewall.batch import SwBatchEntry, _bind
+    L = _bind()
+    tab = (SwBatchEntry * 2)()
+    assert L.sw_batch_graph_run(None, ctypes.addressof(tab), 1, N.SW_F16_SHIFT, 10, None) == N.SW_ERR_BAD_ARG
+    assert L.sw_batch_graph_create(None) == N.SW_ERR_BAD_ARG
+    assert L.sw_batch_graph_destroy(None) == N.SW_OK
+    assert L.sw_batch_graph_launches(None) == -1
