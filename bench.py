@@ -137,6 +137,20 @@ def profiled_traffic(dtype, cells):
     return None
 
 
+def cpu_model():
+    """The host CPU's model name (Linux /proc/cpuinfo; 'model name', or the Arm 'CPU part' line)."""
+    try:
+        with open("/proc/cpuinfo") as fh:
+            text = fh.read()
+    except OSError:
+        return "unknown"
+    for key in ("model name", "Model", "CPU part"):
+        for line in text.splitlines():
+            if line.startswith(key):
+                return line.split(":", 1)[1].strip()
+    return "unknown"
+
+
 # ---------------------------------------------------------------- CPU oracle timing
 def cpu_sample(p, flag, target_s=10.0, max_steps=None):
     """Time the CPU oracle on an x-crop of the workload around the wall.  Returns dict."""
@@ -158,6 +172,7 @@ def cpu_sample(p, flag, target_s=10.0, max_steps=None):
             break
     cells = crop.size
     return dict(value=round(cells * steps / el / 1e6, 2), unit="MLUPS", cores=threads, kind="port",
+                cpu=cpu_model(), host_cpus=os.cpu_count(),
                 sample=f"{steps} float32 steps of an x-crop {nxc}x{p.ny}x{p.nz} ({cells/1e6:.2f} M cells) of the "
                        f"workload around the wall, {el:.1f} s, oracle/sw_oracle.cpp with {threads} OpenMP threads")
 
@@ -206,7 +221,8 @@ def run_reference(a):
                 dtype="f32", data="synthetic", impl="reference",
                 config=dict(workload=a.workload, grid=[p.nx, p.ny, p.nz], H=p.H, porosity=WORKLOADS[a.workload]
                             ["porosity"], sample_grid=[nxc, p.ny, p.nz]),
-                cpu_baseline=dict(value=round(mlups, 2), unit="MLUPS", cores=threads, kind="port", sample=sample),
+                cpu_baseline=dict(value=round(mlups, 2), unit="MLUPS", cores=threads, kind="port", sample=sample,
+                                  cpu=cpu_model(), host_cpus=os.cpu_count()),
                 e2e=dict(value=round(mlups, 2), unit="MLUPS", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
     return 0
@@ -330,6 +346,7 @@ def run_ours(a):
                     config=dict(workload=f"{a.workload}: {p.nx}x{p.ny}x{p.nz} H={p.H} ellipsoid wall porosity "
                                          f"{WORKLOADS[a.workload]['porosity']} seed {WORKLOADS[a.workload]['seed']}",
                                 grid=[p.nx, p.ny, p.nz], cells=cells, fluid_cells=fluid_cells,
+                                fluid_mlups=round(value * fluid_cells / cells, 1),
                                 solid_fraction_of_wall_box=round(frac, 4), phase="averaging (accumulate every 5th)",
                                 l2="no flush: each lattice is %.2f GB > 129 MB L2" % (cells * 76 / 1e9 *
                                                                                         BYTES_PER_CELL[dtype] / 152),
