@@ -116,6 +116,9 @@ class Server:
         self.cap = float(cap_bytes)
         self.max_cells = float(max_cells) if max_cells else float("inf")
         self.cells = 0
+        # the persistent mode's table uploads are double-buffered by events, the graph mode's executable
+        # graphs by the handle: neither needs the device idle between chunks
+        self.persistent_sync = False
         self.chunk = int(chunk)
         self.device = torch.device(device)
         self.batches = {dt: Batch(dtype=dt, chunk=chunk, max_members=max_members, device=device, mode=mode)
@@ -157,7 +160,8 @@ class Server:
         done = [rid for rid, (req, s, need) in self.resident.items() if s.t >= s.n_total]
         for rid in done:
             req, s, need = self.resident.pop(rid)
-            st = solve_stats(s)
+            st = solve_stats(s)                    # reads the force series: waits for the solve's last chunk
+            now = self.clock() - self._t0
             req.result = dict(stats=st, t_done=now, latency=now - req.t_arrive, wait=req.t_admit - req.t_arrive,
                               run=now - req.t_admit, cells=s.grid.cells)
             self.batches[req.dtype].remove(s)
@@ -170,7 +174,7 @@ class Server:
         """Replay the request stream in real time.  Returns the requests (with .result when done)."""
         reqs = sorted(requests, key=lambda r: r.t_arrive)
         queue, prepared = [], {}
-        t0 = self.clock()
+        t0 = self._t0 = self.clock()
         i = 0
         last_log = 0.0
         self.max_used = 0.0
@@ -184,9 +188,10 @@ class Server:
             active = [b for b in self.batches.values() if b.pending()]
             self.max_used = max(self.max_used, self.used)
             if active:
-                for b in active:
-                    b.advance(self.chunk)
-                torch.cuda.synchronize()
+                for b in active:             # enqueued; the host goes on admitting and retiring meanwhile
+                    b.advance(self.chunk)    # (step counts are host-side; a batch keeps <= 2 chunks queued)
+                if self.persistent_sync:
+                    torch.cuda.synchronize()
             else:
                 if i >= len(reqs) and not queue:
                     break
