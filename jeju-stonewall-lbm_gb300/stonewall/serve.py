@@ -313,8 +313,9 @@ def main(argv=None):
     t0 = time.monotonic()
     out = srv.serve(reqs, max_seconds=a.minutes * 60.0, drain=not a.no_drain)
     elapsed = time.monotonic() - t0
-    summ = srv.summary(out, elapsed)
-    summ.update(form="plain" if a.plain else f"batched ({a.mode})", unfinished_at_end=srv.unfinished,
+    summ = Server.summary(out, elapsed)
+    summ.update(form="plain (float32, one at a time)" if a.plain else f"batched ({a.mode})",
+                unfinished_at_end=srv.unfinished,
                 max_resident_gb=round(srv.max_used / 1e9, 2), cap_gb=a.cap_gb, arrivals_per_s=a.rate,
                 window_minutes=a.minutes, seed=a.seed, drained=not a.no_drain)
     if a.fp64_check:

@@ -71,3 +71,16 @@ def test_resident_cells_cap_limits_concurrency(cuda):
     out = srv.serve(reqs)
     assert all(r.result is not None for r in out)
     assert max(seen) <= cap_cells
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_command_line_end_to_end(plain, cuda):
+    from stonewall.serve import main
+    argv = ["--minutes", "0.01", "--rate", "300", "--h-lo", "8", "--h-hi", "10", "--steps-lo", "60",
+            "--steps-hi", "120", "--chunk", "16", "--seed", "5"] + (["--plain"] if plain else ["--fp64-check", "1"])
+    summ = main(argv)
+    assert summ["completed"] == summ["requests"] > 0
+    assert summ["p99_latency_s"] >= summ["p50_latency_s"] >= 0
+    assert summ["form"].startswith("plain" if plain else "batched")
+    if not plain:
+        assert len(summ["fp64_check"]) == 1 and summ["fp64_check"][0]["Cd"] < 0.05
