@@ -144,10 +144,13 @@ def cpu_model():
             text = fh.read()
     except OSError:
         return "unknown"
+    arm_parts = {"0xd4f": "Arm Neoverse-V2", "0xd40": "Arm Neoverse-V1", "0xd0c": "Arm Neoverse-N1",
+                 "0xd49": "Arm Neoverse-N2", "0xd8e": "Arm Neoverse-N3", "0xd84": "Arm Neoverse-V3"}
     for key in ("model name", "Model", "CPU part"):
         for line in text.splitlines():
             if line.startswith(key):
-                return line.split(":", 1)[1].strip()
+                v = line.split(":", 1)[1].strip()
+                return arm_parts.get(v, f"CPU part {v}") if key == "CPU part" else v
     return "unknown"
 
 

@@ -2,7 +2,7 @@
 
     python -m stonewall.profile_launch [--H 40] [--dtype f16] [--cfg 8] [--batch]
 
-The wall is the c2 headline case by default (800 x 160 x 160, H = 40, ellipsoid
+The wall is by default the 800 x 160 x 160 headline case (H = 40, ellipsoid
 wall, porosity 0.2, seed 1, 2 % Gaussian initial noise).  Without --batch the
 single-lattice step runs in launch configuration --cfg (sw_step_cfg); with
 --batch the persistent batched kernel (stonewall.batch.Batch, this wall
