@@ -188,6 +188,23 @@ def dist_env():
     return ws, rank, local
 
 
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws, device="cpu"):
+    """The largest of the ranks' values (the timing rule: the slowest replica sets the step time)."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(a):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -250,16 +267,6 @@ def run_ours(a):
     fluid_cells = int((flag == 0).sum())
     W, Ks = a.warmup, a.steps
 
-    def barrier():
-        if ws > 1:
-            torch.distributed.barrier()
-
-    def max_over_ranks(x):
-        if ws == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
 
     # --- resident run: averaging phase of the solve (step + accumulation every 5th step)
     n_total = p.n_total
@@ -270,7 +277,7 @@ def run_ours(a):
     cfg, cfg_times = solver.autotune()                               # launch configuration, untimed
     solver.advance(max(W, 3 * a.chunk if a.chunk <= Ks else W))    # warm-up, graph capture included
     torch.cuda.synchronize()
-    barrier()
+    barrier(ws)
     launches0 = solver.launches
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -279,8 +286,8 @@ def run_ours(a):
         solver.advance(Ks)
         e1.record()
         torch.cuda.synchronize()
-    barrier()
-    ms = max_over_ranks(e0.elapsed_time(e1))
+    barrier(ws)
+    ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
     gpu_launches = solver.launches - launches0
     value = ws * cells * Ks / (ms * 1e-3) / 1e6
 
@@ -321,7 +328,7 @@ def run_ours(a):
     solver.advance(min(solver.n_total, 2 * a.chunk))               # capture graphs outside the timed region
     force_host = torch.empty((Ks, g.nz, 2), dtype=torch.int64).pin_memory()
     torch.cuda.synchronize()
-    barrier()
+    barrier(ws)
     x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     x0.record()
     solver.reload(flag_pin, uin_pin)        # H2D of the mask and inlet, re-classification
@@ -330,8 +337,8 @@ def run_ours(a):
     force_host.copy_(solver.force.data[:Ks], non_blocking=True)
     x1.record()
     torch.cuda.synchronize()
-    barrier()
-    e2e_ms = max_over_ranks(x0.elapsed_time(x1))
+    barrier(ws)
+    e2e_ms = max_over_ranks(x0.elapsed_time(x1), ws, dev)
     e2e = dict(value=round(ws * cells * Ks / (e2e_ms * 1e-3) / 1e6, 1), unit="MLUPS",
                h2d_bytes_per_step=round((flag.nbytes + p.uin.nbytes) / Ks, 1),
                d2h_bytes_per_step=g.nz * 2 * 8, ms_total=round(e2e_ms, 3))
