@@ -51,3 +51,25 @@ def test_graph_batch_rejects_bad_arguments(native_lib):
     assert L.sw_batch_graph_create(None) == N.SW_ERR_BAD_ARG
     assert L.sw_batch_graph_destroy(None) == N.SW_OK
     assert L.sw_batch_graph_launches(None) == -1
+
+
+def test_driver_derives_the_reference_grid_and_physics():
+    """The CLI's grid, inlet speed, viscosity and step counts against what the reference's own
+    main() recorded for the same flags (driver_small.npz meta, lbm3d.py:269-282)."""
+    import json
+    from conftest import golden
+    from stonewall.driver import derive, parse
+    d = golden("driver_small")
+    meta, argv = json.loads(str(d["meta"])), json.loads(str(d["argv"]))
+    p = derive(parse(argv))
+    assert (p.nx, p.ny, p.nz, p.H, p.T, p.X0) == (meta["nx"], meta["ny"], meta["nz"], meta["H"], meta["T"], meta["X0"])
+    assert (p.n_spin, p.n_avg, p.snap_every) == (meta["n_spin"], meta["n_avg"], meta["snap_every"])
+    assert p.UH == pytest.approx(meta["UH"], rel=1e-12)
+    assert p.nu0 == pytest.approx(meta["nu"], rel=1e-12)
+    assert p.t_unit == pytest.approx(meta["steps_per_unit"], rel=1e-12)
+    H = p.H
+    ds3 = max(1, int(round(H / 13)))
+    q_x0 = max(1, p.X0 - int(round(0.5 * H)))
+    q_dims = [min(int(round(9.0 * H)), p.nx - 1 - q_x0) // ds3, p.ny // ds3, min(int(round(2.5 * H)), p.nz - 1) // ds3]
+    assert meta["q3d"]["x0"] == q_x0 and meta["q3d"]["ds"] == ds3 and meta["q3d"]["dims"] == q_dims
+    assert meta["y_mid"] == p.ny // 2 and meta["z_half"] == int(round(0.5 * H)) + 1
