@@ -18,6 +18,9 @@ Fixtures:
   driver_small.npz  lbm3d.main() end to end on a 32x8x13 grid (H=4, 10 steps,
                     snapshots, a checkpoint, Q-criterion frames); the .npz the
                     reference writes, unchanged, plus its argv
+  driver_small_ckpt.npz  the checkpoint that run writes at step 5 (the
+                    reference removes it when the run completes; kept here
+                    by copying it just before): f, force, uacc, snaps_*, state
   geometry.npz      geometry.build_wall masks (bit-packed) and porosities
 """
 import argparse
@@ -88,10 +91,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--out", default=HERE)
+    ap.add_argument("--only", default="", help="comma-separated fixture names to (re)write (default: all)")
     a = ap.parse_args()
     lbm3d, geometry, wp = load_reference(a.ref)
+    only = set(v for v in a.only.split(",") if v)
 
-    np.savez_compressed(os.path.join(a.out, "tables.npz"), C=lbm3d.C, W=lbm3d.W, OPP=lbm3d.OPP,
+    def wanted(name):
+        return not only or name in only
+
+    if wanted("tables"):
+        np.savez_compressed(os.path.join(a.out, "tables.npz"), C=lbm3d.C, W=lbm3d.W, OPP=lbm3d.OPP,
                         MIRZ=lbm3d.MIRZ, flags=np.array([lbm3d.FLUID, lbm3d.WALL, lbm3d.GROUND]))
 
     # case 1: a stone block, a lone stone beside the top and the periodic edge
@@ -105,7 +114,8 @@ def main():
     uin = inlet_profile(nz, 3, 0.08)
     out = run_steps(lbm3d, wp, flag, uin, nu0=np.float32(0.002), cs=0.1, x_sponge=11, nu_sponge=0.05,
                     n_steps=4, noise=0.02, seed=3)
-    np.savez_compressed(os.path.join(a.out, "step_box.npz"), **out)
+    if wanted("step_box"):
+        np.savez_compressed(os.path.join(a.out, "step_box.npz"), **out)
 
     # case 2: random stones and interior GROUND cells (bounce-back without force)
     print("step_rand", flush=True)
@@ -122,7 +132,8 @@ def main():
     uin = inlet_profile(nz, 2, 0.06)
     out = run_steps(lbm3d, wp, flag, uin, nu0=0.01, cs=0.16, x_sponge=8, nu_sponge=0.05,
                     n_steps=3, noise=0.05, seed=5)
-    np.savez_compressed(os.path.join(a.out, "step_rand.npz"), **out)
+    if wanted("step_rand"):
+        np.savez_compressed(os.path.join(a.out, "step_rand.npz"), **out)
 
     # case 3: the reference driver end to end
     print("driver_small", flush=True)
@@ -132,13 +143,29 @@ def main():
             "--ckpt-every", "5", "--device", "cpu", "--out", tmp]
     old = sys.argv
     sys.argv = argv
+    kept, rmtree = {}, shutil.rmtree
+
+    def keep_then_remove(path, *args, **kw):        # the finished run removes its checkpoint: copy it first
+        if os.path.basename(path) == "g.ckpt" and os.path.isdir(path):
+            kept["g.ckpt"] = shutil.copytree(path, os.path.join(tempfile.mkdtemp(), "g.ckpt"))
+        return rmtree(path, *args, **kw)
+    lbm3d.shutil.rmtree = keep_then_remove
     try:
         lbm3d.main()
     finally:
         sys.argv = old
+        lbm3d.shutil.rmtree = rmtree
     d = dict(np.load(os.path.join(tmp, "g.npz")))
     d["argv"] = np.array(json.dumps(argv[1:-2]))
-    np.savez_compressed(os.path.join(a.out, "driver_small.npz"), **d)
+    if wanted("driver_small"):
+        np.savez_compressed(os.path.join(a.out, "driver_small.npz"), **d)
+    if wanted("driver_small_ckpt"):
+        ck = kept["g.ckpt"]
+        c = {k: np.load(os.path.join(ck, k + ".npy")) for k in ("f", "force", "uacc", "snaps_xz", "snaps_xy",
+                                                                 "snaps_q")}
+        with open(os.path.join(ck, "state.json")) as fh:
+            c["state"] = np.array(fh.read())
+        np.savez_compressed(os.path.join(a.out, "driver_small_ckpt.npz"), **c)
     shutil.rmtree(tmp)
 
     # geometry: the reference's mask producer
@@ -152,7 +179,8 @@ def main():
         g[f"mask{k}"] = np.packbits(m.ravel())
         g[f"spec{k}"] = np.array([por, H, seed, nx, ny, nz, X0, T, phi], np.float64)
     g["n"] = np.array(len(specs))
-    np.savez_compressed(os.path.join(a.out, "geometry.npz"), **g)
+    if wanted("geometry"):
+        np.savez_compressed(os.path.join(a.out, "geometry.npz"), **g)
     print("done", flush=True)
 
 

@@ -22,11 +22,34 @@ def _run_driver(tmp_path, argv):
     return dict(np.load(os.path.join(tmp_path, "g.npz")))
 
 
-def test_driver_matches_reference_main(tmp_path, cuda):
-    d = golden("driver_small")
+def _reference_argv(d):
     argv = json.loads(str(d["argv"]))
     argv[argv.index("--device") + 1] = "cuda"
-    got = _run_driver(tmp_path, argv)
+    return argv
+
+
+def test_driver_matches_reference_main(tmp_path, cuda):
+    d = golden("driver_small")
+    got = _run_driver(tmp_path, _reference_argv(d))
+    _assert_matches_reference(got, d)
+
+
+def test_driver_resumes_a_reference_checkpoint(tmp_path, cuda):
+    """The checkpoint the reference's main() wrote at step 5 (its float32 files, lbm3d.py:342-355)
+    resumed by this driver: the finished outputs equal the reference's uninterrupted run."""
+    d, c = golden("driver_small"), golden("driver_small_ckpt")
+    ck = tmp_path / "g.ckpt"
+    ck.mkdir()
+    for k in ("f", "force", "uacc", "snaps_xz", "snaps_xy", "snaps_q"):
+        np.save(ck / f"{k}.npy", c[k])
+    (ck / "state.json").write_text(str(c["state"]))
+    assert json.loads(str(c["state"]))["t"] == 5
+    got = _run_driver(tmp_path, _reference_argv(d))
+    assert not ck.exists()                                     # removed once the run completed
+    _assert_matches_reference(got, d)
+
+
+def _assert_matches_reference(got, d):
     for k in ("wall_xz", "wall_xy", "wall_front", "wall_top", "wall_ds2"):
         np.testing.assert_array_equal(got[k], d[k], err_msg=k)
     m_ref, m_got = json.loads(str(d["meta"])), json.loads(str(got["meta"]))

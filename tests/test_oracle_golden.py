@@ -103,3 +103,25 @@ def test_oracle_qcoarse_equals_the_per_cell_loop():
                     best = max(best, q_at(x, y, z))
             want[i, j, k] = best
         np.testing.assert_array_equal(O.qcoarse(u, flag, x0, ds, dims), want)
+
+
+def test_reference_checkpoint_continues_to_the_reference_result():
+    """The reference's step-5 checkpoint of the driver case, advanced 5 steps by the oracle from the
+    reference's own mask and parameters, gives the reference run's Cd / Cm for steps 5-9."""
+    import json
+    from oracle import oracle as O
+    from stonewall.driver import derive, parse
+    from stonewall.geometry import course_wall
+    from stonewall.metrics import coefficients
+    from stonewall.params import flags_from_wall
+    d, c = golden("driver_small"), golden("driver_small_ckpt")
+    p = derive(parse(json.loads(str(d["argv"]))))
+    wall, _ = course_wall(0.2, p.H, p.nx, p.ny, p.nz, p.X0, p.T, seed=7)
+    flag = flags_from_wall(wall, p.nx, p.ny, p.nz)
+    t0 = json.loads(str(c["state"]))["t"]
+    f, force = O.run(c["f"], flag, p.uin, np.float32(p.nu0), np.float32(0.16), p.x_sponge, p.n_total - t0,
+                     np.float32(p.nu_sponge))
+    full = np.concatenate([c["force"][:t0].astype(np.float64), force])
+    co = coefficients(full, p.UH, p.H, p.ny, p.zeta)
+    for k in ("Cd", "Cm"):
+        np.testing.assert_allclose(co[k], d[k], rtol=1e-5, atol=1e-6 * np.abs(d[k]).max(), err_msg=k)
