@@ -121,6 +121,9 @@ class Server:
         self.persistent_sync = False
         self.chunk = int(chunk)
         self.device = torch.device(device)
+        if mode == "graph":
+            from .batch import GRAPH_MAX
+            max_members = min(max_members, GRAPH_MAX)
         self.batches = {dt: Batch(dtype=dt, chunk=chunk, max_members=max_members, device=device, mode=mode)
                         for dt in ("f32", "f16")}
         self._tuned = set()
@@ -142,6 +145,9 @@ class Server:
             if self.used + need > self.cap:
                 return
             if self.resident and self.cells + cells_of(req) > self.max_cells:
+                return
+            b = self.batches[req.dtype]
+            if len(b.members) >= b.max_members:           # the batch's table (graph mode: 256 walls) is full
                 return
             queue.pop(0)
             p, flag = fut.result()
