@@ -73,3 +73,40 @@ def test_driver_derives_the_reference_grid_and_physics():
     q_dims = [min(int(round(9.0 * H)), p.nx - 1 - q_x0) // ds3, p.ny // ds3, min(int(round(2.5 * H)), p.nz - 1) // ds3]
     assert meta["q3d"]["x0"] == q_x0 and meta["q3d"]["ds"] == ds3 and meta["q3d"]["dims"] == q_dims
     assert meta["y_mid"] == p.ny // 2 and meta["z_half"] == int(round(0.5 * H)) + 1
+
+
+def test_server_admission_rules(monkeypatch):
+    """First come first served under the byte cap, the resident-cells limit and the batch tables'
+    capacity -- the admission logic alone, with stand-ins for the GPU solvers."""
+    import concurrent.futures as cf
+    from types import SimpleNamespace
+    import stonewall.serve as S
+
+    class FakeBatch:
+        def __init__(self, cap):
+            self.members, self.max_members = [], cap
+
+        def add(self, s):
+            self.members.append(s)
+
+    def fake_solver(req, p, flag, device):
+        return SimpleNamespace(grid=SimpleNamespace(cells=S.cells_of(req)), autotune=lambda: None, t=0,
+                               n_total=req.steps)
+
+    monkeypatch.setattr(S, "make_solver", fake_solver)
+    reqs = S.poisson_requests(5.0, 4.0, seed=11, H_range=(16, 20), steps=(100, 200))
+    done = cf.Future()
+    done.set_result((None, None))
+    srv = object.__new__(S.Server)
+    srv.cap, srv.max_cells, srv.cells, srv.used, srv.device = 3.2 * max(S.footprint(r) for r in reqs), float("inf"), 0, 0.0, None
+    srv.resident, srv._tuned = {}, set()
+    srv.batches = {"f32": FakeBatch(2), "f16": FakeBatch(2)}
+    queue = list(reqs)
+    srv._admit(queue, {r.rid: done for r in reqs}, 0.0)
+    admitted = [r for r in reqs if r.rid in srv.resident]
+    assert admitted == reqs[:len(admitted)]                       # a prefix: first come first served
+    assert srv.used <= srv.cap and all(len(b.members) <= 2 for b in srv.batches.values())
+    nxt = queue[0]
+    blocked_by_table = len(srv.batches[nxt.dtype].members) == 2
+    blocked_by_cap = srv.used + S.footprint(nxt) > srv.cap
+    assert blocked_by_table or blocked_by_cap                     # the head waits for a reason
