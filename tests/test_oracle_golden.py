@@ -125,3 +125,34 @@ def test_reference_checkpoint_continues_to_the_reference_result():
     co = coefficients(full, p.UH, p.H, p.ny, p.zeta)
     for k in ("Cd", "Cm"):
         np.testing.assert_allclose(co[k], d[k], rtol=1e-5, atol=1e-6 * np.abs(d[k]).max(), err_msg=k)
+
+
+def test_course_wall_reproduces_the_reference_masks():
+    """stonewall.geometry.course_wall restates geometry.build_wall (geometry.py:135-161): the same
+    seed gives the same mask and frontal porosity as the reference's own generator."""
+    from stonewall.geometry import course_wall
+    g = golden("geometry")
+    for k in range(int(g["n"])):
+        por, H, seed, nx, ny, nz, X0, T, phi = g[f"spec{k}"]
+        shape = (int(nx), int(ny), int(nz))
+        want = np.unpackbits(g[f"mask{k}"])[:int(np.prod(shape))].reshape(shape).astype(bool)
+        got, got_phi = course_wall(float(por), int(H), *shape, int(X0), int(T), seed=int(seed))
+        np.testing.assert_array_equal(got, want, err_msg=f"mask {k}")
+        assert got_phi == pytest.approx(phi, abs=1e-12), k
+
+
+def test_ellipsoid_wall_properties():
+    """The BASELINE wall generator: seeded, confined to the wall box above the ground, and filled
+    to the target solid fraction within half a stone."""
+    from stonewall.geometry import ellipsoid_wall
+    from stonewall.params import baseline_params
+    for H, por, seed in ((16, 0.2, 0), (24, 0.45, 3), (16, 0.0, 1)):
+        p = baseline_params(H, 1000)
+        a, fa = ellipsoid_wall(por, p.H, p.nx, p.ny, p.nz, p.X0, p.T, seed=seed)
+        b, fb = ellipsoid_wall(por, p.H, p.nx, p.ny, p.nz, p.X0, p.T, seed=seed)
+        np.testing.assert_array_equal(a, b)
+        assert fa == fb
+        outside = a.copy()
+        outside[p.X0:p.X0 + p.T, :, 1:1 + H] = False
+        assert not outside.any()                                   # stones only in the wall box
+        assert abs(fa - (1 - por)) < 0.02
