@@ -22,6 +22,8 @@ Fixtures:
                     reference removes it when the run completes; kept here
                     by copying it just before): f, force, uacc, snaps_*, state
   geometry.npz      geometry.build_wall masks (bit-packed) and porosities
+  postprocess.npz   the reference's Cd / Cm statistics of the driver case and its
+                    reverse-flow area of a seeded mean field
 """
 import argparse
 import json
@@ -85,6 +87,34 @@ def inlet_profile(nz, H, U0):
     uin = (U0 * np.clip(zeta / (3.0 * H), 0, 1) ** (1 / 7)).astype(np.float32)
     uin[0] = 0.0
     return uin
+
+
+def write_postprocess(out, driver_npz):
+    """postprocess.npz: the reference's own Cd / Cm statistics (postprocess.py:46-83, on the driver
+    case's .npz) and reverse-flow area (export3d.py:169-184, on a seeded mean field with a
+    reverse-flow pocket behind a block of stones).  export3d.py imports scikit-image for its
+    meshes, which is not installed: a stand-in marching_cubes returns a one-triangle mesh, which
+    the area does not use."""
+    import types
+    import postprocess
+    m, payload, _ = postprocess.case_payload(driver_npz)
+    meas = types.ModuleType("skimage.measure")
+    meas.marching_cubes = lambda vol, level: (np.zeros((3, 3)), np.array([[0, 1, 2]]), None, None)
+    sk = types.ModuleType("skimage")
+    sk.measure = meas
+    sys.modules.setdefault("skimage", sk)
+    sys.modules.setdefault("skimage.measure", meas)
+    import export3d
+    rng = np.random.default_rng(3)
+    H, X0, nx, ny, nz, UH = 8, 40, 160, 32, 33, 0.05
+    ux = rng.normal(0.03, 0.01, (3, nx // 2, ny // 2, (nz + 1) // 2)).astype(np.float16)
+    ux[0, 22:36, 3:12, 1:6] = -0.01                               # the pocket
+    wall = np.zeros((nx // 2, ny // 2, (nz + 1) // 2), bool)
+    wall[20:23, :, 1:4] = True
+    z = export3d.reverse_zone(dict(mean3d_ds2=ux, wall_ds2=wall), dict(H=H, X0=X0, UH=UH, ny=ny, nx=nx, nz=nz))
+    np.savez_compressed(os.path.join(out, "postprocess.npz"), stats=np.array(json.dumps(payload["stats"])),
+                        n_spin=np.array(m["n_spin"]), ux_ds2=ux, wall_ds2=wall,
+                        params=np.array([H, X0, nx, ny, nz, UH]), area=np.array(z["area"]))
 
 
 def main():
@@ -159,6 +189,8 @@ def main():
     d["argv"] = np.array(json.dumps(argv[1:-2]))
     if wanted("driver_small"):
         np.savez_compressed(os.path.join(a.out, "driver_small.npz"), **d)
+    if wanted("postprocess"):
+        write_postprocess(a.out, os.path.join(tmp, "g.npz"))
     if wanted("driver_small_ckpt"):
         ck = kept["g.ckpt"]
         c = {k: np.load(os.path.join(ck, k + ".npy")) for k in ("f", "force", "uacc", "snaps_xz", "snaps_xy",

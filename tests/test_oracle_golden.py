@@ -156,3 +156,18 @@ def test_ellipsoid_wall_properties():
         outside[p.X0:p.X0 + p.T, :, 1:1 + H] = False
         assert not outside.any()                                   # stones only in the wall box
         assert abs(fa - (1 - por)) < 0.02
+
+
+def test_statistics_and_reverse_flow_area_match_the_reference():
+    """stonewall.metrics against the reference's own postprocess.py statistics (on the driver
+    case's Cd / Cm / Cl series) and export3d.py reverse-flow area (on a seeded mean field)."""
+    import json
+    from stonewall.metrics import recirculation_area, stats
+    g, d = golden("postprocess"), golden("driver_small")
+    want = json.loads(str(g["stats"]))
+    got = stats(d["Cd"], d["Cm"], d["Cl"], int(g["n_spin"]))
+    for k, v in want.items():
+        assert got[k] == pytest.approx(v, rel=1e-6, abs=1e-6), k       # the reference sums in float32
+    H, X0, nx, ny, nz, UH = g["params"]
+    area = recirculation_area(g["ux_ds2"][0], g["wall_ds2"], int(H), int(X0), float(UH), int(ny))
+    assert area > 0 and area == float(g["area"])
