@@ -110,3 +110,22 @@ def test_server_admission_rules(monkeypatch):
     blocked_by_table = len(srv.batches[nxt.dtype].members) == 2
     blocked_by_cap = srv.used + S.footprint(nxt) > srv.cap
     assert blocked_by_table or blocked_by_cap                     # the head waits for a reason
+
+
+@pytest.mark.parametrize("H,n,grid", [(16, 2000, (320, 64, 64)), (40, 40000, (800, 160, 160)),
+                                      (64, 20000, (1280, 256, 256))])
+def test_baseline_workload_parameters(H, n, grid):
+    """The measured workloads: 20H x 4H x 4H, wall 0.75H thick at x = 5H, inlet 0.05 (z/H)^(1/7),
+    Re_H = 1e4, Cs = 0.1; spin-up 20 H/U_H when the run is long enough, else the first 40 %."""
+    from stonewall.params import baseline_params
+    p = baseline_params(H, n)
+    assert (p.nx, p.ny, p.nz) == grid
+    assert (p.X0, p.T) == (5 * H, round(0.75 * H))
+    assert p.UH == 0.05 and p.Cs == 0.1 and p.nu0 == pytest.approx(0.05 * H / 1e4)
+    z = np.arange(p.nz) - 0.5
+    want = (0.05 * np.clip(z / H, 0, None) ** (1 / 7)).astype(np.float32)
+    want[0] = 0.0
+    np.testing.assert_array_equal(p.uin, want)
+    t_unit = H / 0.05
+    assert p.n_spin == (int(20 * t_unit) if n >= 2 * int(20 * t_unit) else int(0.4 * n))
+    assert p.n_spin + p.n_avg == n and p.x_sponge == p.nx - 3 * H
