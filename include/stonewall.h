@@ -17,7 +17,8 @@
  *                              x and z momentum-exchange force per height level
  *                              and step, as force[t][z][0..1] in lbm3d.py:99-101
  * pitch = nx rounded up to a multiple of 32 (sw_geom_make).  Cells with
- * x >= nx are padding and are never read or written by the step.
+ * x >= nx are padding: the step never reads them, and the 16-bit steps may
+ * write don't-care values there (they store cells in aligned pairs).
  *
  * The D3Q19 tables that the reference passes as arrays (cx, cy, cz, w, opp,
  * mirz; lbm3d.py:20-28, 297-300) are compiled in, in the reference's order.
@@ -39,7 +40,7 @@ enum {
   SW_OK = 0,
   SW_ERR_BAD_ARG = 1,     /* null pointer, bad extent, unknown dtype, inconsistent geometry */
   SW_ERR_OOM = 2,         /* reserved for callers that allocate (the library never does) */
-  SW_ERR_NONFINITE = 3,   /* a non-finite density or velocity was found (sw_check_finite) */
+  SW_ERR_NONFINITE = 3,   /* reserved: a diverged state (the Python driver checks the macro field) */
   SW_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
   SW_ERR_CUDA = 5,        /* a CUDA call failed; sw_last_cuda_error() has the code */
   SW_ERR_UNSUPPORTED = 6, /* valid request this build does not implement */
