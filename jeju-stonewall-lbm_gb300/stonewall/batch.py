@@ -24,7 +24,6 @@ and in any mix; tests/test_gpu_batch.py checks this.
 """
 import ctypes
 
-import numpy as np
 import torch
 
 from . import _native as N

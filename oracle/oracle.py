@@ -6,7 +6,6 @@ reference's layout (stonewall3d/lbm3d.py:293-303): f[19, nx, ny, nz],
 flag[nx, ny, nz], u[4, nx, ny, nz], all C-contiguous, z fastest.
 """
 import ctypes
-import os
 
 import numpy as np
 

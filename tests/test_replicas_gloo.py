@@ -9,7 +9,6 @@ import os
 import socket
 import sys
 
-import pytest
 import torch.multiprocessing as mp
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

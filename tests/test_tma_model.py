@@ -8,7 +8,6 @@ this is the source the reference pull names (lbm3d.py:77-97: periodic y, the
 outlet copying its own column, the top mirroring z).  Grids with odd sizes,
 one-row-group widths and a last segment that ends mid-warp.
 """
-import numpy as np
 import pytest
 
 from aa_model import C, MIRZ
