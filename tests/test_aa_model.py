@@ -34,3 +34,27 @@ def test_aa_two_steps_equal_pingpong(shape, seed, density):
     assert problems == []
     fluid = np.broadcast_to(flag == 0, want.shape)
     np.testing.assert_allclose(got[fluid], want[fluid], rtol=1e-12, atol=1e-12)
+
+
+def test_aa_plan_on_generated_masks():
+    """The same property on masks drawn by hypothesis (shapes down to one row, dense and empty
+    stone fills, stones anywhere including the inlet, outlet and top planes)."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True)
+    @hyp.given(nx=st.integers(3, 7), ny=st.integers(1, 4), nz=st.integers(2, 5), seed=st.integers(0, 10 ** 6),
+               density=st.floats(0.0, 0.6))
+    def check(nx, ny, nz, seed, density):
+        rng = np.random.default_rng(seed)
+        flag = (rng.random((nx, ny, nz)) < density).astype(np.uint8)
+        flag[:, :, 0] = 2
+        S = rng.random((19, nx, ny, nz))
+        M = rng.standard_normal((19, 19))
+        want = pingpong_step(pingpong_step(S, flag, M), flag, M)
+        got, problems = aa_two_steps(S, flag, M)
+        assert problems == []
+        fluid = np.broadcast_to(flag == 0, want.shape)
+        np.testing.assert_allclose(got[fluid], want[fluid], rtol=1e-12, atol=1e-12)
+
+    check()

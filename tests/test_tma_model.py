@@ -71,3 +71,19 @@ def test_staged_reads_are_the_pull_sources(shape):
                 for i in range(19):
                     assert staged_source(nx, ny, nz, x, y, z, i) == pull_source(nx, ny, nz, x, y, z, i), \
                         (shape, x, y, z, i)
+
+
+def test_staged_reads_on_generated_grids():
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=15, deadline=None, derandomize=True)
+    @hyp.given(nx=st.integers(2, 140), ny=st.integers(1, 11), nz=st.integers(2, 5))
+    def check(nx, ny, nz):
+        for x in range(1, nx):
+            for y in range(ny):
+                for z in range(1, nz):
+                    for i in range(19):
+                        assert staged_source(nx, ny, nz, x, y, z, i) == pull_source(nx, ny, nz, x, y, z, i)
+
+    check()
