@@ -133,6 +133,10 @@ def main(argv=None):
         print(f"[{a.case}] resumed from step {solver.t} ({solver.t/p.t_unit:.1f} H/U)", flush=True)
     else:
         solver.init(noise=0.02, seed=a.seed, noise_kind=a.noise_dist)
+    # launch configuration for this grid and storage type (times each one on the spare lattice;
+    # the state and the results do not change)
+    cfg, _ = solver.autotune()
+    print(f"[{a.case}] step launch configuration {cfg}", flush=True)
 
     t0 = time.time()
     t_start = solver.t
