@@ -15,6 +15,8 @@ Fixtures:
                     k_init then 4 ping-pong k_step, k_macro and k_accum
   step_rand.npz     12x5x7 grid, random stones plus interior GROUND cells,
                     3 steps with a different viscosity / Cs / sponge
+  step_edge.npz     9x1x3 grid: the span one cell wide (y wraps onto itself),
+                    stones in the top and outlet planes, sponge over half the grid
   driver_small.npz  lbm3d.main() end to end on a 32x8x13 grid (H=4, 10 steps,
                     snapshots, a checkpoint, Q-criterion frames); the .npz the
                     reference writes, unchanged, plus its argv
@@ -164,6 +166,21 @@ def main():
                     n_steps=3, noise=0.05, seed=5)
     if wanted("step_rand"):
         np.savez_compressed(os.path.join(a.out, "step_rand.npz"), **out)
+
+    # case 2b: edges -- a one-cell-wide periodic span (y wraps onto itself), two fluid levels
+    # under the free-slip top, a stone in the top plane and one in the outlet plane, the
+    # reference's default Cs, the sponge covering half the domain
+    print("step_edge", flush=True)
+    nx, ny, nz = 9, 1, 3
+    flag = np.zeros((nx, ny, nz), np.uint8)
+    flag[:, :, 0] = lbm3d.GROUND
+    flag[4, 0, 2] = lbm3d.WALL
+    flag[nx - 1, 0, 1] = lbm3d.WALL
+    uin = inlet_profile(nz, 1, 0.05)
+    out = run_steps(lbm3d, wp, flag, uin, nu0=0.002, cs=0.16, x_sponge=4, nu_sponge=0.05,
+                    n_steps=3, noise=0.04, seed=9)
+    if wanted("step_edge"):
+        np.savez_compressed(os.path.join(a.out, "step_edge.npz"), **out)
 
     # case 3: the reference driver end to end
     print("driver_small", flush=True)

@@ -11,7 +11,7 @@ import pytest
 from conftest import golden
 
 
-@pytest.mark.parametrize("case", ["step_box", "step_rand"])
+@pytest.mark.parametrize("case", ["step_box", "step_rand", "step_edge"])
 def test_oracle_matches_reference_kernels(case, oracle_mod):
     d = golden(case)
     flag, uin = d["flag"], d["uin"]
