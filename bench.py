@@ -54,6 +54,14 @@ WORKLOADS = {
 }
 
 
+def bench_config(name, p, dtype):
+    """The workload description both arms print (same dict, so the two lines can be matched)."""
+    w = WORKLOADS[name]
+    return dict(workload=f"{name}: {p.nx}x{p.ny}x{p.nz} H={p.H} ellipsoid wall porosity {w['porosity']} "
+                         f"seed {w['seed']}", grid=[p.nx, p.ny, p.nz], H=p.H, porosity=w["porosity"], seed=w["seed"],
+                dtype=dtype, phase="averaging (accumulate every 5th step)")
+
+
 def workload(name):
     from stonewall.geometry import ellipsoid_wall
     from stonewall.params import baseline_params, flags_from_wall
@@ -96,6 +104,9 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
             self.thread.join(timeout=2)
+
+    def rows(self):
+        return len(self.lines)
 
     def summary(self):
         rows = []
@@ -239,8 +250,8 @@ def run_reference(a):
     line = dict(metric=METRIC, value=round(mlups, 2), unit="MLUPS", n_gpus=a.gpus, steps=a.steps, warmup=a.warmup,
                 ms_per_step=round(el / a.steps * 1e3, 3), higher_is_better=True, scaling="weak", vs_baseline=None,
                 dtype="f32", data="synthetic", impl="reference",
-                config=dict(workload=a.workload, grid=[p.nx, p.ny, p.nz], H=p.H, porosity=WORKLOADS[a.workload]
-                            ["porosity"], sample_grid=[nxc, p.ny, p.nz]),
+                config=bench_config(a.workload, p, "f32"),
+                sample_grid=[nxc, p.ny, p.nz],
                 cpu_baseline=dict(value=round(mlups, 2), unit="MLUPS", cores=threads, kind="port", sample=sample,
                                   cpu=cpu_model(), host_cpus=os.cpu_count()),
                 e2e=dict(value=round(mlups, 2), unit="MLUPS", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
@@ -260,22 +271,28 @@ def run_ours(a):
     from stonewall import _native
     from stonewall import kernels as K
     from stonewall.solver import WallSolver
-    _native.lib()
+    L = _native.lib()
     p, flag, frac = workload(a.workload)
     dtype = a.dtype
     cells = p.cells
     fluid_cells = int((flag == 0).sum())
     W, Ks = a.warmup, a.steps
-
+    chunk = min(a.chunk, Ks)          # the timed steps replay CUDA graphs of `chunk` steps
 
     # --- resident run: averaging phase of the solve (step + accumulation every 5th step)
     n_total = p.n_total
     solver = WallSolver(flag, p.uin, p.nu0, p.Cs, p.x_sponge, n_total, n_spin=0, dtype=dtype, device=dev,
-                        chunk=a.chunk)
+                        chunk=chunk)
     solver.init(noise=0.02, seed=1, noise_kind="gauss")
     solver.advance(W)
-    cfg, cfg_times = solver.autotune()                               # launch configuration, untimed
-    solver.advance(max(W, 3 * a.chunk if a.chunk <= Ks else W))    # warm-up, graph capture included
+    if a.cfg is None:
+        cfg, cfg_times = solver.autotune()                           # launch configuration, untimed
+        cfg_acc = L.sw_get_step_config_accum(solver.dtype)
+    else:
+        _native.check(L.sw_set_step_config(solver.dtype, a.cfg), "sw_set_step_config")
+        _native.check(L.sw_set_step_config_accum(solver.dtype, a.cfg), "sw_set_step_config_accum")
+        cfg, cfg_acc, cfg_times = a.cfg, a.cfg, {}
+    solver.advance(max(W, 2 * chunk))                                # warm-up, graph capture included
     torch.cuda.synchronize()
     barrier(ws)
     launches0 = solver.launches
@@ -283,12 +300,29 @@ def run_ours(a):
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         e0.record()
-        solver.advance(Ks)
+        solver.advance(Ks, check=False)      # graph replays; the status word is read after e1
         e1.record()
         torch.cuda.synchronize()
+        solver.check_status()
+        gpu_launches = solver.launches - launches0
+        clocks = clk.summary()
+        if clocks is None or clocks["samples"] < 3:
+            # the timed region was shorter than three sampling intervals: sample the same steps,
+            # continued right after it, for about a second (untimed)
+            t_end = time.perf_counter() + 1.0
+            while (time.perf_counter() < t_end or clk.rows() < 3) and time.perf_counter() < t_end + 5.0:
+                if solver.t + chunk > solver.n_total:
+                    break
+                solver.advance(chunk, check=False)
+                torch.cuda.synchronize()
+            clocks = clk.summary()
+            if clocks is not None:
+                clocks["sampled"] = ("the same steps continued for ~1 s right after the timed region, which is "
+                                     "shorter than three 200 ms sampling intervals")
+        else:
+            clocks["sampled"] = "during the timed region"
     barrier(ws)
     ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
-    gpu_launches = solver.launches - launches0
     value = ws * cells * Ks / (ms * 1e-3) / 1e6
 
     # --- roofline: the step kernel alone, eager launches on this stream
@@ -298,12 +332,14 @@ def run_ours(a):
         K.k_step(src, dst, solver.flags, solver.uin, g.nx, g.ny, g.nz, p.nu0, p.Cs, p.x_sponge, 0.05, None, 0)
         src, dst = dst, src
     torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
     r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    r0.record()
+    r0.record(stream)
     for i in range(Ks):
-        K.k_step(src, dst, solver.flags, solver.uin, g.nx, g.ny, g.nz, p.nu0, p.Cs, p.x_sponge, 0.05, None, 0)
+        K.k_step(src, dst, solver.flags, solver.uin, g.nx, g.ny, g.nz, p.nu0, p.Cs, p.x_sponge, 0.05, None, 0,
+                 stream=stream)
         src, dst = dst, src
-    r1.record()
+    r1.record(stream)
     torch.cuda.synchronize()
     step_ms = r0.elapsed_time(r1) / Ks
     alg_bytes = BYTES_PER_CELL[dtype] * fluid_cells
@@ -322,10 +358,10 @@ def run_ours(a):
     # --- end to end through the public API, host buffers in and out
     flag_pin = torch.from_numpy(flag).pin_memory()
     uin_pin = torch.from_numpy(p.uin.copy()).pin_memory()
-    solver = WallSolver(flag, p.uin, p.nu0, p.Cs, p.x_sponge, max(Ks, a.chunk), n_spin=0, dtype=dtype,
-                        device=dev, chunk=a.chunk)
+    solver = WallSolver(flag, p.uin, p.nu0, p.Cs, p.x_sponge, max(Ks, 2 * chunk), n_spin=0, dtype=dtype,
+                        device=dev, chunk=chunk)
     solver.init(noise=0.02, seed=1, noise_kind="gauss")
-    solver.advance(min(solver.n_total, 2 * a.chunk))               # capture graphs outside the timed region
+    solver.advance(min(solver.n_total, 2 * chunk))                 # capture graphs outside the timed region
     force_host = torch.empty((Ks, g.nz, 2), dtype=torch.int64).pin_memory()
     torch.cuda.synchronize()
     barrier(ws)
@@ -333,7 +369,7 @@ def run_ours(a):
     x0.record()
     solver.reload(flag_pin, uin_pin)        # H2D of the mask and inlet, re-classification
     solver.init(noise=0.02, seed=1, noise_kind="gauss")
-    solver.advance(Ks)
+    solver.advance(Ks)                      # reads the status word at the end
     force_host.copy_(solver.force.data[:Ks], non_blocking=True)
     x1.record()
     torch.cuda.synchronize()
@@ -341,7 +377,7 @@ def run_ours(a):
     e2e_ms = max_over_ranks(x0.elapsed_time(x1), ws, dev)
     e2e = dict(value=round(ws * cells * Ks / (e2e_ms * 1e-3) / 1e6, 1), unit="MLUPS",
                h2d_bytes_per_step=round((flag.nbytes + p.uin.nbytes) / Ks, 1),
-               d2h_bytes_per_step=g.nz * 2 * 8, ms_total=round(e2e_ms, 3))
+               d2h_bytes_per_step=g.nz * 2 * 8 + 4, ms_total=round(e2e_ms, 3))
     del solver
     torch.cuda.empty_cache()
 
@@ -352,18 +388,17 @@ def run_ours(a):
     if rank == 0:
         line = dict(metric=METRIC, value=round(value, 1), unit="MLUPS", n_gpus=ws, steps=Ks, warmup=W,
                     ms_per_step=round(ms / Ks, 4), higher_is_better=True, scaling="weak", vs_baseline=None,
-                    dtype=dtype, data="synthetic",
-                    config=dict(workload=f"{a.workload}: {p.nx}x{p.ny}x{p.nz} H={p.H} ellipsoid wall porosity "
-                                         f"{WORKLOADS[a.workload]['porosity']} seed {WORKLOADS[a.workload]['seed']}",
-                                grid=[p.nx, p.ny, p.nz], cells=cells, fluid_cells=fluid_cells,
-                                fluid_mlups=round(value * fluid_cells / cells, 1),
-                                solid_fraction_of_wall_box=round(frac, 4), phase="averaging (accumulate every 5th)",
-                                l2="no flush: each lattice is %.2f GB > 129 MB L2" % (cells * 76 / 1e9 *
-                                                                                        BYTES_PER_CELL[dtype] / 152),
-                                graph_chunk=a.chunk, parallelism=f"replicas x{ws}", step_config=cfg,
-                                step_config_ms={str(k): round(v, 4) for k, v in cfg_times.items()}),
+                    dtype=dtype, data="synthetic", config=bench_config(a.workload, p, dtype),
+                    run=dict(cells=cells, fluid_cells=fluid_cells, fluid_mlups=round(value * fluid_cells / cells, 1),
+                             solid_fraction_of_wall_box=round(frac, 4),
+                             l2="no flush: each lattice is %.2f GB > 129 MB L2" % (cells * 76 / 1e9 *
+                                                                                    BYTES_PER_CELL[dtype] / 152),
+                             timed_steps=f"{Ks} steps as {Ks // chunk} replays of a {chunk}-step CUDA graph"
+                                         + (f" + {Ks % chunk} eager launches" if Ks % chunk else ""),
+                             parallelism=f"replicas x{ws}", step_config=cfg, step_config_accum=cfg_acc,
+                             step_config_ms={str(k): round(v, 4) for k, v in cfg_times.items()}),
                     roofline=roofline, cpu_baseline=cpu, e2e=e2e, gpu_launches=gpu_launches,
-                    clocks=clk.summary())
+                    clocks=clocks)
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -381,6 +416,8 @@ def main(argv=None):
     ap.add_argument("--chunk", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cfg", type=int, default=None,
+                    help="use this step launch configuration instead of autotuning (for profiling commands)")
     a = ap.parse_args(argv)
     if a.warmup < 3:
         ap.error("--warmup must be at least 3")

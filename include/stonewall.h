@@ -40,11 +40,22 @@ enum {
   SW_OK = 0,
   SW_ERR_BAD_ARG = 1,     /* null pointer, bad extent, unknown dtype, inconsistent geometry */
   SW_ERR_OOM = 2,         /* reserved for callers that allocate (the library never does) */
-  SW_ERR_NONFINITE = 3,   /* reserved: a diverged state (the Python driver checks the macro field) */
+  SW_ERR_NONFINITE = 3,   /* a diverged state (sw_status_error of SW_STATUS_NONFINITE) */
   SW_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
   SW_ERR_CUDA = 5,        /* a CUDA call failed; sw_last_cuda_error() has the code */
   SW_ERR_UNSUPPORTED = 6, /* valid request this build does not implement */
   SW_ERR_TOO_LARGE = 7    /* grid exceeds the fixed scratch of sw_step_noalloc */
+};
+
+/* Bits of a lattice's device status word (uint32_t in device memory).  The
+ * checked step entry points (sw_step_checked, sw_step_aa, batch entries with a
+ * status pointer) OR them in; the caller zeroes the word and reads it back
+ * when it wants to know, e.g. once per run of steps.  The reference detects
+ * divergence on the host, from the macro field every 5000 steps
+ * (lbm3d.py:386-391); here every fluid cell of every step is covered. */
+enum {
+  SW_STATUS_NONFINITE = 1, /* some fluid cell had a non-finite density after pulling its populations */
+  SW_STATUS_TIMEOUT = 2    /* a block of the TMA-staged step gave up waiting for its copies: cells unwritten */
 };
 
 /* storage type of the distributions */
@@ -151,6 +162,27 @@ int sw_get_step_config_accum(int dtype);
 int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
                 const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge,
                 int64_t *force, int64_t t, double *acc, int cfg, sw_stream s);
+/* k_step with the failure checks of lbm3d.py:386-391 moved onto the device:
+ * as sw_step_cfg, and every fluid cell whose pulled density is not finite, and
+ * every TMA-staged block that gave up waiting, ORs SW_STATUS_NONFINITE /
+ * SW_STATUS_TIMEOUT into *status (a device word the caller owns and clears;
+ * NULL: no checks, as sw_step_cfg).  cfg -1 takes the configuration installed
+ * for the storage type (sw_set_step_config, or ..._accum when acc is given). */
+int sw_step_checked(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
+                    const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge,
+                    double nu_sponge, int64_t *force, int64_t t, double *acc, int cfg, uint32_t *status,
+                    sw_stream s);
+/* The error a status word read back from the device stands for: SW_OK (0),
+ * SW_ERR_TIMEOUT (checked first: the cells of a timed-out block were not
+ * written) or SW_ERR_NONFINITE. */
+int sw_status_error(uint32_t word);
+/* Test hook, no reference counterpart: the polls a TMA-staged block makes on
+ * a stage's copies before it gives up (default 16384, microseconds apart).
+ * With 0 every block of the next TMA-staged launches gives up at once, lets
+ * the copies it issued land (that wait keeps its normal bound) and reports
+ * SW_STATUS_TIMEOUT, which is how the time-out path is tested without a
+ * device fault.  Returns the previous value; a negative argument only reads. */
+int32_t sw_debug_tma_poll_limit(int32_t polls);
 
 /* AA pattern: the same step on ONE lattice, updated in place (half the
  * memory of f_in + f_out).  No reference counterpart: the reference always
@@ -162,11 +194,12 @@ int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, cons
  * lattice is in transit and can only be advanced by the even step.  ghost:
  * sw_aa_ghost_elems(g) stored values of scratch, written and read by the odd
  * step.  acc may be NULL (otherwise as sw_step_accum).  States, forces and
- * sums after every even step equal the two-lattice step's bit for bit. */
+ * sums after every even step equal the two-lattice step's bit for bit.
+ * status: as sw_step_checked (NULL: no checks). */
 int64_t sw_aa_ghost_elems(const sw_geom *g);
 int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t *flag, const uint8_t *tiles,
                const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
-               int64_t t, double *acc, void *ghost, sw_stream s);
+               int64_t t, double *acc, void *ghost, uint32_t *status, sw_stream s);
 
 /* k_macro, lbm3d.py:158-182 (lbm3d.py:367, 387): u = (rho, ux, uy, uz); solids -> (1, 0, 0, 0). */
 int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s);
@@ -202,6 +235,7 @@ typedef struct sw_batch_entry {
   int32_t cur0;          /* buffer (0 or 1) holding the state at k = 0 */
   int64_t t0;            /* step index of launch k = 0 */
   int64_t steps_left;    /* launches with k >= steps_left leave the lattice untouched */
+  uint32_t *status;      /* the lattice's device status word (SW_STATUS_*), or NULL: no checks */
 } sw_batch_entry;
 
 typedef struct sw_batch_header {
@@ -223,8 +257,9 @@ int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_de
                   sw_stream s);
 
 /* The same batch as one CUDA graph of single-lattice launches: per entry a
- * chain of min(k_steps, steps_left) sw_step / sw_step_accum launches (the
- * storage type's configurations from sw_set_step_config[_accum]), the chains
+ * chain of min(k_steps, steps_left) sw_step_checked launches (the storage
+ * type's configurations from sw_set_step_config[_accum]; accumulating on the
+ * entry's accumulation steps; checks into the entry's status word), the chains
  * parallel branches between a fork and a join, so lattices run concurrently
  * under the hardware block scheduler.  entries is a HOST table (item0 and
  * items are not used; no sw_batch_prepare needed), at most
@@ -269,11 +304,15 @@ int sw_qcoarse(const sw_geom *g, const float *u, const uint8_t *flag, int32_t x0
  * library holds it until the process exits), rebuilt from `flag` on each call.
  *   - grids with more than SW_NOALLOC_MAX_SEGMENTS segments (nz*ny*pitch/32,
  *     about 134 M cells) are rejected with SW_ERR_TOO_LARGE;
- *   - nothing is allocated, neither by the library nor by the CUDA runtime on
- *     its behalf;
+ *   - the entry point calls no allocating routine.  The array itself comes
+ *     into existence with the library's device code on that device: at the
+ *     first call per device under CUDA's default lazy module loading (or when
+ *     the library loads, with CUDA_MODULE_LOADING=EAGER);
  *   - the first call on a device looks up the array's device address (once per
- *     device, with that device current): make that first call before any
- *     stream capture;
+ *     device, with that device current) and caches it: make that first call
+ *     before any stream capture.  cudaDeviceReset destroys the array with the
+ *     context; the cached address is then stale, so do not call this entry
+ *     point on a device after resetting it;
  *   - all calls on a device share the array: calls that overlap on the GPU
  *     (other streams, other host threads) race and must be serialised. */
 #define SW_NOALLOC_MAX_SEGMENTS (1 << 22)

@@ -183,9 +183,9 @@ __device__ __forceinline__ void aa_odd_cell(const StepParams &p, const AAParams 
     });
     rho = R(1.0); ux = u0; uy = R(0.0); uz = R(0.0);
   } else {
-    const R cs = (R)p.cs;
-    collide<R, S::kShift>(fl, x, (R)p.nu0, R(18.0) * sqrt(R(2.0)) * cs * cs, p.x_sponge, (R)p.sponge_scale,
-                          (R)p.nu_sponge, rho, ux, uy, uz, scatter);
+    const Phys<R> ph = phys<R>(p);
+    collide<R, S::kShift>(fl, x, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz,
+                          p.status, scatter);
   }
   if (ACC) {
     atomicAdd(p.accp(0) + c, (double)rho);
@@ -251,9 +251,9 @@ __device__ __forceinline__ void aa_even_cell(const StepParams &p, int x, int y, 
         }
       });
     }
-    const R cs = (R)p.cs;
-    collide<R, S::kShift>(fl, x, (R)p.nu0, R(18.0) * sqrt(R(2.0)) * cs * cs, p.x_sponge, (R)p.sponge_scale,
-                          (R)p.nu_sponge, rho, ux, uy, uz, put);
+    const Phys<R> ph = phys<R>(p);
+    collide<R, S::kShift>(fl, x, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz,
+                          p.status, put);
   }
   if (ACC) {
     atomicAdd(p.accp(0) + c, (double)rho);
@@ -298,6 +298,7 @@ cudaError_t launch_aa(const StepParams &p_in, const AAParams &a, bool odd, cudaS
   if (p_in.g.nz > 65535 || (p_in.g.ny + 3) / 4 > 65535) return cudaErrorInvalidValue;
   StepParams p = p_in;
   set_plane_bases(p, sizeof(T));                    // fin == fout == the lattice: natural plane bases
+  set_float_params(p);
   const size_t pb = (size_t)p.g.plane * sizeof(T);
   for (int i = 0; i < Q; ++i) {
     if (odd) p.fout_pop[i] = static_cast<char *>(p.fout) + (size_t)OPP(i) * pb;

@@ -26,8 +26,10 @@ struct BatchCtx {
   const uint8_t *tiles;
   const float *uin;
   double nu0, cs, nu_sponge, sponge_scale;
+  float nu0f, c18f, sponge_scalef, nu_spongef;   // as StepParams (set_float_params)
   int x_sponge;
   long long *force;
+  unsigned int *status;     // the lattice's status word, or nullptr
   const void *fin_pop[Q];   // plane bases, filled once per lattice
   void *fout_pop[Q];
   double *acc_pop[4];
@@ -103,6 +105,11 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
         sc.nu_sponge = e.nu_sponge;
         sc.x_sponge = e.x_sponge;
         sc.sponge_scale = (e.geom.nx != e.x_sponge) ? 1.0 / (double)(e.geom.nx - e.x_sponge) : 0.0;
+        sc.nu0f = (float)e.nu0;
+        sc.c18f = smag_c18f((float)e.cs);
+        sc.sponge_scalef = (float)sc.sponge_scale;
+        sc.nu_spongef = (float)e.nu_sponge;
+        sc.status = e.status;
         const long long t = e.t0 + k;
         sc.force = e.force ? reinterpret_cast<long long *>(e.force) + t * 2 * e.geom.nz : nullptr;
         s_acc = e.acc != nullptr && t >= e.n_spin && (t - e.n_spin) % e.acc_every == 0;

@@ -2,7 +2,7 @@
 //
 // The second way to advance many lattices together (the first is the
 // persistent kernel of sw_batch.cuh).  Each lattice gets a chain of K
-// launches of the single-lattice step (sw_step / sw_step_accum, with the
+// launches of the single-lattice step (sw_step_checked: sw_step / sw_step_accum with the
 // storage type's tuned launch configuration, its own __grid_constant__
 // parameters and the hardware block scheduler), and the chains are captured
 // on separate streams, so they are parallel branches of one graph between a
@@ -123,12 +123,9 @@ int sw_batch_graph_run(sw_batch_graph *g, const sw_batch_entry *entries, int32_t
       const long long t = b.t0 + k;
       const int cur = (b.cur0 + k) & 1;
       sw_stream bs = reinterpret_cast<sw_stream>(g->branch[i]);
-      if (accumulates(b, t))
-        rc = sw_step_accum(&b.geom, dtype, b.f[cur], b.f[cur ^ 1], b.flag, b.tiles, b.uin, b.nu0, b.cs, b.x_sponge,
-                           b.nu_sponge, b.force, t, b.acc, bs);
-      else
-        rc = sw_step(&b.geom, dtype, b.f[cur], b.f[cur ^ 1], b.flag, b.tiles, b.uin, b.nu0, b.cs, b.x_sponge,
-                     b.nu_sponge, b.force, t, bs);
+      // the storage type's installed configuration (plain or accumulating), checks into b.status
+      rc = sw_step_checked(&b.geom, dtype, b.f[cur], b.f[cur ^ 1], b.flag, b.tiles, b.uin, b.nu0, b.cs, b.x_sponge,
+                           b.nu_sponge, b.force, t, accumulates(b, t) ? b.acc : nullptr, -1, b.status, bs);
       ++launches;
     }
   }

@@ -135,14 +135,26 @@ namespace {
 // launch configurations used by sw_step and by sw_step_accum, per storage type
 int g_step_cfg[4] = {0, 0, 0, 0};
 int g_step_cfg_acc[4] = {0, 0, 0, 0};
+// polls of a TMA-staged block on one stage before it gives up (sw_debug_tma_poll_limit)
+int g_tma_poll_limit = 1 << 14;
+
+void fill_physics(sw::StepParams &p, const sw_geom *g, double nu0, double cs, int32_t x_sponge, double nu_sponge) {
+  p.nu0 = nu0;
+  p.cs = cs;
+  p.nu_sponge = nu_sponge;
+  p.x_sponge = x_sponge;
+  p.sponge_scale = (g->nx != x_sponge) ? 1.0 / (double)(g->nx - x_sponge) : 0.0;
+}
 
 int step_impl(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
               const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
-              int64_t t, double *acc, int cfg, sw_stream s) {
+              int64_t t, double *acc, int cfg, uint32_t *status, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f_in || !f_out || !flag || !tiles || !uin) return SW_ERR_BAD_ARG;
+  if (cfg == -1) cfg = acc ? g_step_cfg_acc[dtype] : g_step_cfg[dtype];
   if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
   if (!sw::step_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
   if (f_in == f_out || !aligned16(f_in) || !aligned16(f_out) || t < 0) return SW_ERR_BAD_ARG;
+  if (status && ((uintptr_t)status & 3u)) return SW_ERR_BAD_ARG;
   sw::StepParams p;
   p.fin = f_in;
   p.fout = f_out;
@@ -150,14 +162,12 @@ int step_impl(const sw_geom *g, int dtype, const void *f_in, void *f_out, const 
   p.tiles = tiles;
   p.uin = uin;
   p.g = to_geom(g);
-  p.nu0 = nu0;
-  p.cs = cs;
-  p.nu_sponge = nu_sponge;
-  p.x_sponge = x_sponge;
-  p.sponge_scale = (g->nx != x_sponge) ? 1.0 / (double)(g->nx - x_sponge) : 0.0;
+  fill_physics(p, g, nu0, cs, x_sponge, nu_sponge);
   p.force = force ? reinterpret_cast<long long *>(force) + (size_t)t * 2 * g->nz : nullptr;
   p.acc = acc;
+  p.status = status;
   p.cfg = cfg;
+  p.tma_poll_limit = g_tma_poll_limit;
   cudaError_t e;
   switch (dtype) {
     case SW_F32: e = sw::step_f32(p, st(s)); break;
@@ -174,7 +184,7 @@ int sw_step(const sw_geom *g, int dtype, const void *f_in, void *f_out, const ui
             const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force, int64_t t,
             sw_stream s) {
   return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, nullptr,
-                   dtype_ok(dtype) ? g_step_cfg[dtype] : 0, s);
+                   dtype_ok(dtype) ? g_step_cfg[dtype] : 0, nullptr, s);
 }
 
 int sw_step_accum(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
@@ -182,13 +192,36 @@ int sw_step_accum(const sw_geom *g, int dtype, const void *f_in, void *f_out, co
                   int64_t *force, int64_t t, double *acc, sw_stream s) {
   if (!acc) return SW_ERR_BAD_ARG;
   return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, acc,
-                   dtype_ok(dtype) ? g_step_cfg_acc[dtype] : 0, s);
+                   dtype_ok(dtype) ? g_step_cfg_acc[dtype] : 0, nullptr, s);
 }
 
 int sw_step_cfg(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag, const uint8_t *tiles,
                 const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
                 int64_t t, double *acc, int cfg, sw_stream s) {
-  return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, acc, cfg, s);
+  if (cfg < 0) return SW_ERR_BAD_ARG;
+  return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, acc, cfg,
+                   nullptr, s);
+}
+
+int sw_step_checked(const sw_geom *g, int dtype, const void *f_in, void *f_out, const uint8_t *flag,
+                    const uint8_t *tiles, const float *uin, double nu0, double cs, int32_t x_sponge,
+                    double nu_sponge, int64_t *force, int64_t t, double *acc, int cfg, uint32_t *status,
+                    sw_stream s) {
+  if (cfg < -1) return SW_ERR_BAD_ARG;
+  return step_impl(g, dtype, f_in, f_out, flag, tiles, uin, nu0, cs, x_sponge, nu_sponge, force, t, acc, cfg,
+                   status, s);
+}
+
+int sw_status_error(uint32_t word) {
+  if (word & SW_STATUS_TIMEOUT) return SW_ERR_TIMEOUT;
+  if (word & SW_STATUS_NONFINITE) return SW_ERR_NONFINITE;
+  return SW_OK;
+}
+
+int32_t sw_debug_tma_poll_limit(int32_t polls) {
+  const int32_t old = g_tma_poll_limit;
+  if (polls >= 0) g_tma_poll_limit = polls;
+  return old;
 }
 
 int sw_step_config_count(void) { return sw::kStepConfigs; }
@@ -292,10 +325,11 @@ int64_t sw_aa_ghost_elems(const sw_geom *g) {
 
 int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t *flag, const uint8_t *tiles,
                const float *uin, double nu0, double cs, int32_t x_sponge, double nu_sponge, int64_t *force,
-               int64_t t, double *acc, void *ghost, sw_stream s) {
+               int64_t t, double *acc, void *ghost, uint32_t *status, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !tiles || !uin || !ghost || !aligned16(f) || t < 0)
     return SW_ERR_BAD_ARG;
   if (odd != 0 && odd != 1) return SW_ERR_BAD_ARG;
+  if (status && ((uintptr_t)status & 3u)) return SW_ERR_BAD_ARG;
   sw::StepParams p;
   p.fin = f;
   p.fout = f;
@@ -303,14 +337,12 @@ int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t 
   p.tiles = tiles;
   p.uin = uin;
   p.g = to_geom(g);
-  p.nu0 = nu0;
-  p.cs = cs;
-  p.nu_sponge = nu_sponge;
-  p.x_sponge = x_sponge;
-  p.sponge_scale = (g->nx != x_sponge) ? 1.0 / (double)(g->nx - x_sponge) : 0.0;
+  fill_physics(p, g, nu0, cs, x_sponge, nu_sponge);
   p.force = force ? reinterpret_cast<long long *>(force) + (size_t)t * 2 * g->nz : nullptr;
   p.acc = acc;
+  p.status = status;
   p.cfg = 0;
+  p.tma_poll_limit = g_tma_poll_limit;
   sw::AAParams a{ghost, ghost};
   cudaError_t e;
   switch (dtype) {

@@ -8,7 +8,9 @@
 // of fixed size instead, so the caller passes only the inputs and outputs.
 //
 // The array (SW_NOALLOC_MAX_SEGMENTS bytes) exists on every GPU that loads the
-// library, for the life of the process.  Every call on a device shares it and
+// library's device code (at the first call there under lazy module loading),
+// for the life of the process, or until cudaDeviceReset destroys the context:
+// the address cached below is not re-queried after a reset.  Every call on a device shares it and
 // rewrites the part its grid uses before reading it, so calls on one device
 // that overlap in time on the GPU (different streams, or different host
 // threads) race with each other and must be serialised by the caller.

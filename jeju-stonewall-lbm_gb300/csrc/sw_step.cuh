@@ -40,10 +40,15 @@ struct StepParams {
   Geom g;
   double nu0, cs, nu_sponge;
   double sponge_scale;  // 1 / (nx - x_sponge)
+  // float copies for the float collision (set_float_params): rounded once on
+  // the host instead of converted from double in every thread
+  float nu0f, c18f, sponge_scalef, nu_spongef;
   int x_sponge;
   long long *force;  // force row of this step: [nz][2], or nullptr
   double *acc;       // float64 running sums [4][plane] (accumulation steps only)
+  unsigned int *status;  // device status word (SW_STATUS_*), or nullptr: no checks
   int cfg;           // launch configuration (SW_STEP_CONFIGS)
+  int tma_poll_limit;  // polls before a TMA-staged block gives up on a stage (set at launch)
   // per-population plane bases (fin + i * plane etc.), uniform across the grid,
   // so that every load and store needs only a 32-bit offset within a plane
   const void *fin_pop[Q];
@@ -68,6 +73,44 @@ inline void set_plane_bases(StepParams &p, size_t elem_bytes) {
   for (int k = 0; k < 4; ++k) p.acc_pop[k] = p.acc ? p.acc + (size_t)k * p.g.plane : nullptr;
 }
 
+// 18 sqrt(2) Cs^2 of the Smagorinsky time scale (lbm3d.py:144-146), evaluated
+// in the order the float kernels evaluated it in-thread, so the rounded value
+// is the same bits on the host and on the device.
+__host__ __device__ inline float smag_c18f(float cs) {
+  float c = 18.0f * sqrtf(2.0f);
+  c = c * cs;
+  return c * cs;
+}
+
+// The float copies of the physics parameters (host side, once per launch).
+inline void set_float_params(StepParams &p) {
+  p.nu0f = (float)p.nu0;
+  p.c18f = smag_c18f((float)p.cs);
+  p.sponge_scalef = (float)p.sponge_scale;
+  p.nu_spongef = (float)p.nu_sponge;
+}
+
+// Physics parameters in the collision's arithmetic type R.
+template <typename R> struct Phys {
+  R nu0, c18, sponge_scale, nu_sponge;
+};
+template <typename R, typename Ctx> __device__ __forceinline__ Phys<R> phys(const Ctx &p) {
+  if constexpr (sizeof(R) == 4) {
+    return {p.nu0f, p.c18f, p.sponge_scalef, p.nu_spongef};
+  } else {
+    const R cs = p.cs;
+    return {p.nu0, R(18.0) * sqrt(R(2.0)) * cs * cs, p.sponge_scale, p.nu_sponge};
+  }
+}
+
+// ORs status bits into the lattice's status word (a rare branch: divergence or a time-out).
+template <typename Ctx> __device__ __forceinline__ void note_status(const Ctx &p, unsigned int bits) {
+  if (p.status != nullptr) atomicOr(p.status, bits);
+}
+// |v| <= largest finite value: false for infinities and NaN.
+__device__ __forceinline__ bool finite_val(float v) { return fabsf(v) <= 3.402823466e38f; }
+__device__ __forceinline__ bool finite_val(double v) { return fabs(v) <= 1.7976931348623157e308; }
+
 // float: the hardware approximations (relative error about 2^-23, far below the
 // 1e-5 parity bar); double: IEEE division and square root.
 __device__ __forceinline__ float rcp(float v) {
@@ -89,9 +132,13 @@ __device__ __forceinline__ double fsqrt(double v) { return sqrt(v); }
 // sum_i w_i c_i = 0 and sum_i w_i c_i c_i = I/3, the moments of g are rho - 1,
 // m and Pi - I/3, so r0 = sum_i f[i] below is rho - 1 (shifted) or rho, and
 // Pi_neq = P - r0/3 I - m m / rho holds in both cases.
+// status: the lattice's status word (or nullptr).  A cell whose pulled density
+// is not finite reports SW_STATUS_NONFINITE there, in a rare branch taken
+// where rho is formed, so that no value stays live for the check.
 template <typename R, bool SHIFT, typename Put>
 __device__ __forceinline__ void collide(const R (&f)[Q], int x, R nu0, R cs2_18r2, int x_sponge, R sponge_scale,
-                                        R nu_sponge, R &rho_out, R &ux_out, R &uy_out, R &uz_out, Put &&put) {
+                                        R nu_sponge, R &rho_out, R &ux_out, R &uy_out, R &uz_out, unsigned int *status,
+                                        Put &&put) {
   // pair sums / differences, pair k = directions (2k+1, 2k+2), c(2k+2) = -c(2k+1)
   R s[9], d[9];
 #pragma unroll
@@ -102,6 +149,7 @@ __device__ __forceinline__ void collide(const R (&f)[Q], int x, R nu0, R cs2_18r
   // pairs: 0 (1,0,0) 1 (0,1,0) 2 (0,0,1) 3 (1,1,0) 4 (1,-1,0) 5 (1,0,1) 6 (1,0,-1) 7 (0,1,1) 8 (0,1,-1)
   const R r0 = f[0] + (((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7])) + s[8]);
   const R rho = SHIFT ? r0 + R(1.0) : r0;
+  if (!finite_val(r0) && status != nullptr) atomicOr(status, (unsigned int)SW_STATUS_NONFINITE);
   const R mx = (d[0] + d[3]) + (d[4] + d[5]) + d[6];
   const R my = (d[1] + d[3]) - d[4] + (d[7] + d[8]);
   const R mz = (d[2] + d[5]) - d[6] + (d[7] - d[8]);
@@ -262,9 +310,9 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
     }
   });
   R rho, ux, uy, uz;
-  const R cs = (R)p.cs;
-  collide<R, S::kShift>(fl, x, (R)p.nu0, R(18.0) * sqrt(R(2.0)) * cs * cs, p.x_sponge, (R)p.sponge_scale,
-                        (R)p.nu_sponge, rho, ux, uy, uz, [&](auto I, R v) {
+  const Phys<R> ph = phys<R>(p);
+  collide<R, S::kShift>(fl, x, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz, p.status,
+                        [&](auto I, R v) {
                           constexpr int i = decltype(I)::value;
                           S::template st<i>(out(i) + c, v);
                         });
@@ -338,10 +386,11 @@ __device__ __forceinline__ f2 operator*(f2 a, f2 b) { return {__fmul2_rn(a.v, b.
 __device__ __forceinline__ f2 operator-(f2 a, f2 b) { return {__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)}; }
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
 
+// status: as collide; both densities are checked (the second only when has_b: past the row end it is padding).
 template <typename Put>
-__device__ __forceinline__ void collide2(const f2 (&f)[Q], int x0, float nu0, float cs2_18r2, int x_sponge,
-                                         float sponge_scale, float nu_sponge, f2 &rho_out, f2 &ux_out, f2 &uy_out,
-                                         f2 &uz_out, Put &&put) {
+__device__ __forceinline__ void collide2(const f2 (&f)[Q], int x0, bool has_b, float nu0, float cs2_18r2,
+                                         int x_sponge, float sponge_scale, float nu_sponge, f2 &rho_out, f2 &ux_out,
+                                         f2 &uy_out, f2 &uz_out, unsigned int *status, Put &&put) {
   f2 s[9], d[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
@@ -350,6 +399,8 @@ __device__ __forceinline__ void collide2(const f2 (&f)[Q], int x0, float nu0, fl
   }
   const f2 r0 = f[0] + (((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7])) + s[8]);
   const f2 rho = r0 + F2(1.0f);
+  if (!finite_val(fabsf(r0.v.x) + (has_b ? fabsf(r0.v.y) : 0.0f)) && status != nullptr)
+    atomicOr(status, (unsigned int)SW_STATUS_NONFINITE);
   const f2 mx = (d[0] + d[3]) + (d[4] + d[5]) + d[6];
   const f2 my = (d[1] + d[3]) - d[4] + (d[7] + d[8]);
   const f2 mz = (d[2] + d[5]) - d[6] + (d[7] - d[8]);
@@ -462,11 +513,10 @@ __device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q
   using S = Store<DT>;
   using T = typename S::T;
   using PK = Pack16<DT>;
-  const float cs = (float)p.cs;
-  const float c18 = 18.0f * sqrtf(2.0f) * cs * cs;
+  const Phys<float> ph = phys<float>(p);
   f2 rho, ux, uy, uz;
-  collide2(v, x0, (float)p.nu0, c18, p.x_sponge, (float)p.sponge_scale, (float)p.nu_sponge, rho, ux, uy, uz,
-           [&](auto I, f2 o) {
+  collide2(v, x0, x0 + 1 < p.g.nx, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz,
+           p.status, [&](auto I, f2 o) {
              constexpr int i = decltype(I)::value;
              __stcs(reinterpret_cast<unsigned int *>(p.template out<T>(i) + c), PK::pack(o.v.x, o.v.y));
            });
@@ -626,6 +676,7 @@ cudaError_t launch_step(const StepParams &p_in, cudaStream_t s) {
   if (p_in.g.nz > 65535 || (p_in.g.ny + 3) / 4 > 65535) return cudaErrorInvalidValue;
   StepParams p = p_in;
   set_plane_bases(p, sizeof(typename Store<DT>::T));
+  set_float_params(p);
   switch (p.cfg) {
 #define SW_CASE(ID, WY, MINB)                                                                      \
   case ID:                                                                                         \

@@ -84,10 +84,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return done != 0;
 }
-// Bounded wait: 2^14 polls with back-off (a copy lands in microseconds; this gives up
-// after milliseconds), then false.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int k = 0; k < (1 << 14); ++k) {
+// Bounded wait: `polls` polls with back-off (the default 2^14: a copy lands in
+// microseconds, this gives up after milliseconds), then false.
+constexpr int kTmaPolls = 1 << 14;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int polls = kTmaPolls) {
+  for (int k = 0; k < polls; ++k) {
     if (mbar_try_wait(bar, parity)) return true;
     if (k > 64) __nanosleep(64);
   }
@@ -179,6 +180,7 @@ template <int DT, bool ACC, typename Cfg>
 __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     k_step_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap map1,
                const __grid_constant__ StepParams p) {
+  static_assert(2 * Cfg::ITEMS <= 32, "one lane per tile byte of the block's items");
   extern __shared__ __align__(128) uint8_t smem_raw[];
   __shared__ __align__(8) unsigned long long bars[Cfg::NSTAGE];
   uint8_t *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);   // 128-byte aligned boxes
@@ -198,30 +200,38 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     for (int j = 0; j < Cfg::NSTAGE && j < n_items; ++j)
       tma_issue(&map, &map1, g, x0s, (yb0 + j) * 4, z, base + j * kTmaStageBytes, smem_u32(&bars[j]));
   }
+  // The segment classes of this warp's rows in all its items, fetched once up
+  // front (lane j: segment 2 bx of item j, lane ITEMS + j: segment 2 bx + 1),
+  // so their latency overlaps the first copies instead of following each wait.
+  uint32_t kinds = TILE_ALL_SOLID;
+  {
+    const int j = lane < Cfg::ITEMS ? lane : lane - Cfg::ITEMS;
+    const int sx = 2 * bx + (lane < Cfg::ITEMS ? 0 : 1);
+    const int y = (yb0 + j) * 4 + w;
+    if (lane < 2 * Cfg::ITEMS && j < n_items && y < g.ny && sx < g.nseg_x)
+      kinds = __ldg(p.tiles + ((size_t)(z * g.ny + y) * g.nseg_x + sx));
+  }
   __syncthreads();
+  const int polls = p.tma_poll_limit;
   bool ok = true;
   int j = 0;
   for (; j < n_items; ++j) {
     const int s = j % Cfg::NSTAGE;
     const uint32_t st = base + s * kTmaStageBytes;
     const int y = (yb0 + j) * 4 + w;
-    if (ok) ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((j / Cfg::NSTAGE) & 1));
-    if (ok && y < g.ny) {
-      const int seg = (z * g.ny + y) * g.nseg_x + 2 * bx;
-      const bool has_tb = 2 * bx + 1 < g.nseg_x;
-      const uint8_t ka = __ldg(p.tiles + seg);
-      const uint8_t kb = has_tb ? __ldg(p.tiles + seg + 1) : (uint8_t)TILE_ALL_SOLID;
-      if (!(ka & kb & TILE_ALL_SOLID)) {
-        const int x0 = x0s + 2 * lane;
-        if (!((ka | kb) & TILE_CHECK)) {
-          tma_pair_fast<DT, ACC>(p, smem + s * kTmaStageBytes, x0, y, z, w, lane);
-        } else {                                                      // next to stones / ground: per cell
-          float fxw = 0.0f, fzw = 0.0f;
-          int hit = 0;
-          if (x0 < g.nx) step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
-          if (x0 + 1 < g.nx) step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
-          if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
-        }
+    const uint8_t ka = (uint8_t)__shfl_sync(0xffffffffu, kinds, j);
+    const uint8_t kb = (uint8_t)__shfl_sync(0xffffffffu, kinds, Cfg::ITEMS + j);
+    if (ok) ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((j / Cfg::NSTAGE) & 1), polls);
+    if (ok && y < g.ny && !(ka & kb & TILE_ALL_SOLID)) {
+      const int x0 = x0s + 2 * lane;
+      if (!((ka | kb) & TILE_CHECK)) {
+        tma_pair_fast<DT, ACC>(p, smem + s * kTmaStageBytes, x0, y, z, w, lane);
+      } else {                                                        // next to stones / ground: per cell
+        float fxw = 0.0f, fzw = 0.0f;
+        int hit = 0;
+        if (x0 < g.nx) step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
+        if (x0 + 1 < g.nx) step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
+        if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
       }
     }
     ok = __syncthreads_and(ok);                                       // stage s is free again
@@ -231,6 +241,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
   }
   if (!ok && leader) {                                                // item j failed: items j .. j+NSTAGE-1
     atomicAdd(&g_tma_timeouts, 1u);                                   // were issued; let their copies land
+    note_status(p, SW_STATUS_TIMEOUT);                                // (with the normal bound)
     for (int k = j; k < n_items && k < j + Cfg::NSTAGE; ++k)
       (void)mbar_wait(smem_u32(&bars[k % Cfg::NSTAGE]), (uint32_t)((k / Cfg::NSTAGE) & 1));
   }

@@ -12,6 +12,8 @@ LIB_PATH = os.path.join(HERE, "libstonewall.so")
 
 # status codes / dtypes / flags (include/stonewall.h)
 SW_OK, SW_ERR_BAD_ARG, SW_ERR_OOM, SW_ERR_NONFINITE, SW_ERR_TIMEOUT, SW_ERR_CUDA, SW_ERR_UNSUPPORTED = range(7)
+SW_ERR_TOO_LARGE = 7
+SW_STATUS_NONFINITE, SW_STATUS_TIMEOUT = 1, 2
 SW_F32, SW_F64, SW_F16_SHIFT, SW_BF16_SHIFT = range(4)
 SW_NOISE_UNIFORM, SW_NOISE_GAUSSIAN = 0, 1
 FORCE_SCALE = 2.0 ** 40
@@ -84,13 +86,17 @@ def lib():
         "sw_step_accum": ([G, ctypes.c_int, P, P, P, P, P, f64, f64, i32, f64, P, i64, P, P], ctypes.c_int),
         "sw_step_cfg": ([G, ctypes.c_int, P, P, P, P, P, f64, f64, i32, f64, P, i64, P, ctypes.c_int, P],
                         ctypes.c_int),
+        "sw_step_checked": ([G, ctypes.c_int, P, P, P, P, P, f64, f64, i32, f64, P, i64, P, ctypes.c_int, P, P],
+                            ctypes.c_int),
+        "sw_status_error": ([ctypes.c_uint32], ctypes.c_int),
+        "sw_debug_tma_poll_limit": ([i32], i32),
         "sw_step_config_count": ([], ctypes.c_int),
         "sw_set_step_config": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "sw_get_step_config": ([ctypes.c_int], ctypes.c_int),
         "sw_set_step_config_accum": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "sw_get_step_config_accum": ([ctypes.c_int], ctypes.c_int),
         "sw_aa_ghost_elems": ([G], i64),
-        "sw_step_aa": ([G, ctypes.c_int, P, i32, P, P, P, f64, f64, i32, f64, P, i64, P, P, P], ctypes.c_int),
+        "sw_step_aa": ([G, ctypes.c_int, P, i32, P, P, P, f64, f64, i32, f64, P, i64, P, P, P, P], ctypes.c_int),
         "sw_macro": ([G, ctypes.c_int, P, P, P, P], ctypes.c_int),
         "sw_accum": ([G, P, P, P], ctypes.c_int),
         "sw_macro_accum": ([G, ctypes.c_int, P, P, P, P, P], ctypes.c_int),

@@ -23,32 +23,43 @@ def config_count():
 
 def time_configs(solver, repeats=8, warmup=2, acc=None):
     """Mean step time in ms of every configuration on the solver's grid (with `acc`, an Accum
-    that receives throw-away sums, the accumulating variant)."""
+    that receives throw-away sums, the accumulating variant).  A configuration whose TMA-staged
+    blocks gave up waiting for their copies (a time-out in its status word or in
+    sw_tma_timeouts) computed an invalid step and is left out, so it can never win by skipping work."""
+    from .fields import StatusWord
     L = N.lib()
     g = solver.grid
     src, dst = solver.f[solver.cur], solver.f[1 - solver.cur]
     stream = torch.cuda.current_stream()
     accp = acc.ptr if acc is not None else None
+    status = StatusWord(device=solver.device)
     res = {}
     for cfg in range(config_count()):
-        if L.sw_step_cfg(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
-                         solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge, None, 0, accp,
-                         cfg, _stream(stream)) == N.SW_ERR_UNSUPPORTED:
-            continue                                  # not compiled for this storage type
+        status.clear()
+        L.sw_tma_timeouts()                           # read and clear the process-wide counter
 
         def launch():
-            N.check(L.sw_step_cfg(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
-                                  solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge,
-                                  None, 0, accp, cfg, _stream(stream)), "sw_step_cfg")
-        for _ in range(warmup):
-            launch()
+            return L.sw_step_checked(g.gp, src.dtype, src.ptr, dst.ptr, solver.flags.ptr, solver.flags.tiles_ptr,
+                                     solver.uin.ptr, solver.nu0, solver.cs, solver.x_sponge, solver.nu_sponge,
+                                     None, 0, accp, cfg, status.ptr, _stream(stream))
+        rc = launch()
+        if rc == N.SW_ERR_UNSUPPORTED:
+            continue                                  # not compiled for this storage type
+        N.check(rc, "sw_step_checked")
+        for _ in range(warmup - 1):
+            N.check(launch(), "sw_step_checked")
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(repeats):
-            launch()
+            N.check(launch(), "sw_step_checked")
         e1.record()
         torch.cuda.synchronize()
+        timed_out = bool(status.read() & N.SW_STATUS_TIMEOUT)
+        if L.sw_tma_timeouts() != 0 or timed_out:      # (reading the counter also clears it)
+            continue
         res[cfg] = e0.elapsed_time(e1) / repeats
+    if not res:
+        raise RuntimeError("no launch configuration completed a step without a device wait time-out")
     return res
 
 

@@ -27,7 +27,7 @@ import ctypes
 import torch
 
 from . import _native as N
-from .fields import _stream
+from .fields import StatusWord, _stream
 
 
 class SwBatchEntry(ctypes.Structure):
@@ -36,7 +36,8 @@ class SwBatchEntry(ctypes.Structure):
                 ("uin", ctypes.c_void_p), ("force", ctypes.c_void_p), ("acc", ctypes.c_void_p),
                 ("nu0", ctypes.c_double), ("cs", ctypes.c_double), ("nu_sponge", ctypes.c_double),
                 ("x_sponge", ctypes.c_int32), ("n_spin", ctypes.c_int32), ("acc_every", ctypes.c_int32),
-                ("cur0", ctypes.c_int32), ("t0", ctypes.c_int64), ("steps_left", ctypes.c_int64)]
+                ("cur0", ctypes.c_int32), ("t0", ctypes.c_int64), ("steps_left", ctypes.c_int64),
+                ("status", ctypes.c_void_p)]
 
 
 class SwBatchHeader(ctypes.Structure):
@@ -102,6 +103,7 @@ class Batch:
             raise ValueError("mode is 'persistent' or 'graph'")
         self.mode = mode
         self._handle = None
+        self._scratch_status = StatusWord(device=self.device)   # tuning launches report here
         _bind()
 
     def __del__(self):
@@ -154,6 +156,7 @@ class Batch:
             e.uin = m.uin.data.data_ptr()
             e.force = None if tuning else m.force.data.data_ptr()
             e.acc = None if tuning else m.acc.data.data_ptr()
+            e.status = (self._scratch_status if tuning else m.status).data.data_ptr()
             e.nu0, e.cs, e.nu_sponge = m.nu0, m.cs, m.nu_sponge
             e.x_sponge, e.n_spin, e.acc_every, e.cur0 = m.x_sponge, m.n_spin, m.acc_every, m.cur
             e.t0 = m.t
@@ -197,9 +200,40 @@ class Batch:
         N.check(N.lib().sw_batch_graph_run(self._graph_handle(), ctypes.addressof(self._table_host[slot]), n_live,
                                            self.dtype, int(c), _stream(None)), "sw_batch_graph_run")
 
+    # ------------------------------------------------------------ failures
+    def status_words(self, members=None):
+        """The members' status words gathered on the device (one int32 each, in member order)."""
+        ms = self.members if members is None else members
+        if not ms:
+            return torch.zeros(0, dtype=torch.int32, device=self.device)
+        return torch.cat([m.status.data for m in ms])
+
+    def failures(self, members=None):
+        """{member: Diverged | DeviceWaitTimeout} for members whose steps reported a failure so far.
+        One gather and one read of all status words (waits for the queued steps)."""
+        from .solver import status_exception
+        ms = list(self.members if members is None else members)
+        words = self.status_words(ms).cpu().tolist()
+        out = {}
+        for m, w in zip(ms, words):
+            err = status_exception(w, f"batch member at step {m.t}")
+            if err is not None:
+                out[m] = err
+        return out
+
+    def check(self):
+        """Raise the first member failure, if any."""
+        bad = self.failures()
+        if bad:
+            raise next(iter(bad.values()))
+        return True
+
     # ------------------------------------------------------------ stepping
-    def advance(self, n, use_graphs=True):
-        """Advance every unfinished member by up to n steps (each stops at its own n_total)."""
+    def advance(self, n, use_graphs=True, check=False):
+        """Advance every unfinished member by up to n steps (each stops at its own n_total).  With
+        check, the members' status words are read at the end and a failure raises; without (the
+        default, as the solve server advances), the steps stay queued and failures are read with
+        failures() when the caller chooses."""
         n = int(n)
         while n > 0:
             c = min(self.chunk, n)
@@ -223,12 +257,14 @@ class Batch:
                 m.t += s
                 m.cur ^= (s & 1)
             n -= c
+        if check:
+            self.check()
         return self
 
     def run(self):
-        """Advance until every member has finished."""
+        """Advance until every member has finished; a member's failure raises."""
         while self.pending():
-            self.advance(self.chunk * 20)
+            self.advance(self.chunk * 20, check=True)
         return self
 
     def cells(self):

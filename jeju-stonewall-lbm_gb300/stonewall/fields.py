@@ -208,3 +208,29 @@ class ForceSeries:
             raise ValueError(f"force has shape {f.shape}, expected {(self.n_steps, self.nz, 2)}")
         self.data.copy_(torch.from_numpy(np.rint(f * N.FORCE_SCALE).astype(np.int64)))
         return self
+
+
+class StatusWord:
+    """A lattice's device status word: the checked step kernels OR SW_STATUS_NONFINITE (a fluid
+    cell pulled a non-finite density) and SW_STATUS_TIMEOUT (a TMA-staged block gave up waiting)
+    into it.  This is the device side of the reference's divergence check (lbm3d.py:386-391),
+    which looks at the macro field every 5000 steps; here every fluid cell of every step counts."""
+
+    def __init__(self, device="cuda"):
+        self.data = torch.zeros(1, dtype=torch.int32, device=device)
+
+    @property
+    def ptr(self):
+        return _ptr(self.data)
+
+    def clear(self):
+        self.data.zero_()
+        return self
+
+    def read(self):
+        """The word's bits (waits for the work queued so far on the current stream)."""
+        return int(self.data.item()) & 0xFFFFFFFF
+
+    def error(self, word=None):
+        """SW_OK, SW_ERR_TIMEOUT or SW_ERR_NONFINITE for the word (read now if not given)."""
+        return N.lib().sw_status_error(self.read() if word is None else int(word))

@@ -21,7 +21,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .fields import Accum, Flags, ForceSeries, Lattice, Macro, _ptr, _stream
+from .fields import Accum, Flags, ForceSeries, Lattice, Macro, StatusWord, _ptr, _stream
 from .lattice import check_tables
 
 
@@ -66,11 +66,14 @@ def k_init(f: Lattice, flag: Flags, uin, noise=0.02, seed=7, noise_kind="uniform
 
 
 def k_step(f_in: Lattice, f_out: Lattice, flag: Flags, uin, nx, ny, nz, nu0, cs, x_sponge, nu_sponge=0.05,
-           force: ForceSeries = None, t=0, stream=None, acc: Accum = None):
+           force: ForceSeries = None, t=0, stream=None, acc: Accum = None, status: StatusWord = None, cfg=None):
     """lbm3d.py:57-155: one fused timestep f_in -> f_out; force[t] receives the wall force.
 
     With ``acc`` the new state's (rho, u) of every fluid cell is also added to
     the running sums (k_macro + k_accum of lbm3d.py:367-369 in the same pass).
+    With ``status`` (a StatusWord) the step reports non-finite densities and
+    TMA wait time-outs into it (sw_step_checked); ``cfg`` picks a launch
+    configuration instead of the installed one.
     """
     g = _same_grid(f_in, f_out, flag)
     if (int(nx), int(ny), int(nz)) != (g.nx, g.ny, g.nz):
@@ -82,7 +85,16 @@ def k_step(f_in: Lattice, f_out: Lattice, flag: Flags, uin, nx, ny, nz, nu0, cs,
         if force.nz != g.nz or not (0 <= int(t) < force.n_steps):
             raise ValueError(f"step {t} outside the force series ({force.n_steps} x {force.nz})")
         fptr = force.ptr
-    if acc is None:
+    if status is not None or cfg is not None:
+        if acc is not None:
+            _same_grid(f_in, acc)
+        N.check(N.lib().sw_step_checked(g.gp, f_in.dtype, f_in.ptr, f_out.ptr, flag.ptr, flag.tiles_ptr,
+                                        _uin(uin).ptr, float(nu0), float(cs), int(x_sponge), float(nu_sponge),
+                                        fptr, int(t), acc.ptr if acc is not None else None,
+                                        -1 if cfg is None else int(cfg),
+                                        status.ptr if status is not None else None, _stream(stream)),
+                "sw_step_checked")
+    elif acc is None:
         N.check(N.lib().sw_step(g.gp, f_in.dtype, f_in.ptr, f_out.ptr, flag.ptr, flag.tiles_ptr, _uin(uin).ptr,
                                 float(nu0), float(cs), int(x_sponge), float(nu_sponge), fptr, int(t),
                                 _stream(stream)), "sw_step")
@@ -94,7 +106,8 @@ def k_step(f_in: Lattice, f_out: Lattice, flag: Flags, uin, nx, ny, nz, nu0, cs,
 
 
 def k_step_aa(f: Lattice, odd, flag: Flags, uin, nu0, cs, x_sponge, nu_sponge=0.05,
-              force: ForceSeries = None, t=0, ghost=None, acc: Accum = None, stream=None):
+              force: ForceSeries = None, t=0, ghost=None, acc: Accum = None, stream=None,
+              status: StatusWord = None):
     """One AA-pattern step on a single lattice, in place (see include/stonewall.h, sw_step_aa)."""
     g = _same_grid(f, flag)
     if ghost is None or ghost.numel() < N.lib().sw_aa_ghost_elems(g.gp) * N.DTYPE_BYTES[f.dtype]:
@@ -106,7 +119,8 @@ def k_step_aa(f: Lattice, odd, flag: Flags, uin, nu0, cs, x_sponge, nu_sponge=0.
         fptr = force.ptr
     N.check(N.lib().sw_step_aa(g.gp, f.dtype, f.ptr, int(bool(odd)), flag.ptr, flag.tiles_ptr,
                                _uin(uin).ptr, float(nu0), float(cs), int(x_sponge), float(nu_sponge), fptr, int(t),
-                               acc.ptr if acc is not None else None, _ptr(ghost), _stream(stream)), "sw_step_aa")
+                               acc.ptr if acc is not None else None, _ptr(ghost),
+                               status.ptr if status is not None else None, _stream(stream)), "sw_step_aa")
 
 
 def k_macro(f: Lattice, flag: Flags, u: Macro, stream=None):

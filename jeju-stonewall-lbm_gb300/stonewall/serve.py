@@ -18,7 +18,11 @@ storage type (fp32 or fp16-shifted, by a seeded coin).  The server:
     step chains on parallel branches; or the persistent batched kernel), so
     requests that arrive while others run join at the next chunk boundary;
   * retires finished solves (force series -> Cd, Cm statistics), frees their
-    memory and admits more.
+    memory and admits more;
+  * fails a solve whose steps reported a non-finite density or a device wait
+    time-out (its status word, read at retirement and every few chunks for
+    all residents): that request alone gets a failure result, is retired at
+    once and counts as not completed; the others are unaffected.
 
 Reported: p50 / p99 time-to-result (arrival to result), queueing and run
 times, solves per hour over the run, GPU throughput.  A solve's result does
@@ -41,7 +45,7 @@ from .batch import Batch
 from .geometry import ellipsoid_wall
 from .metrics import coefficients, stats
 from .params import baseline_params, flags_from_wall
-from .solver import WallSolver
+from .solver import DeviceWaitTimeout, Diverged, WallSolver
 
 DTYPE_BYTES = {"f32": 4, "f16": 2, "bf16": 2, "f64": 8}
 
@@ -104,6 +108,12 @@ def make_solver(req, p, flag, device="cuda"):
     return s
 
 
+def failure_result(req, s, err, now):
+    """The result of a request whose solve failed (diverged or timed out)."""
+    return dict(failed=type(err).__name__, error=str(err), t_done=now, latency=now - req.t_arrive,
+                wait=req.t_admit - req.t_arrive, run=now - req.t_admit, cells=s.grid.cells, steps_done=s.t)
+
+
 def solve_stats(s):
     p = s.params
     co = coefficients(s.force_series(), p.UH, p.H, p.ny)
@@ -112,7 +122,7 @@ def solve_stats(s):
 
 class Server:
     def __init__(self, cap_bytes=160e9, chunk=50, max_members=256, device="cuda", workers=4, clock=time.monotonic,
-                 mode="graph", max_cells=None):
+                 mode="graph", max_cells=None, check_every=20):
         self.cap = float(cap_bytes)
         self.max_cells = float(max_cells) if max_cells else float("inf")
         self.cells = 0
@@ -129,6 +139,8 @@ class Server:
         self._tuned = set()
         self.pool = cf.ThreadPoolExecutor(max_workers=workers)
         self.clock = clock
+        self.check_every = int(check_every)       # loop iterations between status checks of all residents
+        self.failed = 0
         self.resident = {}                         # rid -> (request, solver, bytes)
         self.used = 0.0
         self.log = []
@@ -162,17 +174,41 @@ class Server:
             self.cells += s.grid.cells
             req.t_admit = now
 
+    def _release(self, rid):
+        req, s, need = self.resident.pop(rid)
+        self.batches[req.dtype].remove(s)
+        self.used -= need
+        self.cells -= s.grid.cells
+        return req, s
+
+    def _fail(self, rid, err):
+        req, s = self._release(rid)
+        req.result = failure_result(req, s, err, self.clock() - self._t0)
+        self.failed += 1
+
+    def _check_residents(self):
+        """Read every resident's status word (one gather per batch) and fail the ones that report."""
+        for b in self.batches.values():
+            if not b.members:
+                continue
+            bad = b.failures()
+            for rid, (req, s, need) in list(self.resident.items()):
+                if s in bad:
+                    self._fail(rid, bad[s])
+
     def _retire(self, now):
         done = [rid for rid, (req, s, need) in self.resident.items() if s.t >= s.n_total]
         for rid in done:
-            req, s, need = self.resident.pop(rid)
+            req, s, need = self.resident[rid]
             st = solve_stats(s)                    # reads the force series: waits for the solve's last chunk
+            err = s.status_error()
+            if err is not None:
+                self._fail(rid, err)
+                continue
+            req, s = self._release(rid)
             now = self.clock() - self._t0
             req.result = dict(stats=st, t_done=now, latency=now - req.t_arrive, wait=req.t_admit - req.t_arrive,
                               run=now - req.t_admit, cells=s.grid.cells)
-            self.batches[req.dtype].remove(s)
-            self.used -= need
-            self.cells -= s.grid.cells
             del s
         return len(done)
 
@@ -184,7 +220,9 @@ class Server:
         i = 0
         last_log = 0.0
         self.max_used = 0.0
+        it = 0
         while True:
+            it += 1
             now = self.clock() - t0
             while i < len(reqs) and reqs[i].t_arrive <= now:
                 queue.append(reqs[i])
@@ -202,6 +240,8 @@ class Server:
                 if i >= len(reqs) and not queue:
                     break
                 time.sleep(0.005)
+            if self.check_every and it % self.check_every == 0 and self.resident:
+                self._check_residents()
             now = self.clock() - t0
             self._retire(now)
             if max_seconds is not None and now > max_seconds and not drain:
@@ -219,7 +259,8 @@ class Server:
 
     @staticmethod
     def summary(reqs, elapsed):
-        done = [r for r in reqs if r.result is not None]
+        failed = [r for r in reqs if r.result is not None and "failed" in r.result]
+        done = [r for r in reqs if r.result is not None and "failed" not in r.result]
         lat = np.array([r.result["latency"] for r in done]) if done else np.zeros(1)
         wait = np.array([r.result["wait"] for r in done]) if done else np.zeros(1)
         cell_steps = sum(r.result["cells"] * r.steps for r in done)
@@ -229,7 +270,8 @@ class Server:
                     p99_latency_s=round(float(np.percentile(lat, 99)), 2),
                     p50_wait_s=round(float(np.percentile(wait, 50)), 2),
                     mean_glups=round(cell_steps / elapsed / 1e9, 2) if elapsed > 0 else 0.0,
-                    f16_share=round(np.mean([r.dtype == "f16" for r in done]), 3) if done else 0.0)
+                    f16_share=round(np.mean([r.dtype == "f16" for r in done]), 3) if done else 0.0,
+                    failed=len(failed))
 
 
 class PlainServer:
@@ -268,7 +310,12 @@ class PlainServer:
             if not tuned:
                 s.autotune()
                 tuned = True
-            s.advance(req.steps)
+            try:
+                s.advance(req.steps)                     # reads the status word at the end
+            except (Diverged, DeviceWaitTimeout) as err:
+                req.result = failure_result(req, s, err, self.clock() - t0)
+                del s
+                continue
             st = solve_stats(s)
             now = self.clock() - t0
             req.result = dict(stats=st, t_done=now, latency=now - req.t_arrive, wait=req.t_admit - req.t_arrive,
@@ -325,7 +372,8 @@ def main(argv=None):
                 max_resident_gb=round(srv.max_used / 1e9, 2), cap_gb=a.cap_gb, arrivals_per_s=a.rate,
                 window_minutes=a.minutes, seed=a.seed, drained=not a.no_drain)
     if a.fp64_check:
-        done = sorted([r for r in out if r.result is not None], key=lambda r: r.H * r.steps)[:a.fp64_check]
+        done = sorted([r for r in out if r.result is not None and "failed" not in r.result],
+                      key=lambda r: r.H * r.steps)[:a.fp64_check]
         errs = []
         for r in done:
             ref = run_alone(Request(rid=r.rid, t_arrive=r.t_arrive, H=r.H, porosity=r.porosity, U=r.U, steps=r.steps,

@@ -24,12 +24,29 @@ import threading
 import numpy as np
 import torch
 
+from . import _native as N
 from . import kernels as K
-from .fields import Accum, Flags, ForceSeries, Grid, Lattice, Macro
+from .fields import Accum, Flags, ForceSeries, Grid, Lattice, Macro, StatusWord
 
 
 class Diverged(RuntimeError):
-    pass
+    """The solve produced a non-finite state (lbm3d.py:386-391 exits with "diverged")."""
+    status = N.SW_ERR_NONFINITE
+
+
+class DeviceWaitTimeout(RuntimeError):
+    """A bounded device wait of the TMA-staged step gave up: the step's results are not valid."""
+    status = N.SW_ERR_TIMEOUT
+
+
+def status_exception(word, where):
+    """The exception a non-zero status word stands for (None for 0)."""
+    err = N.lib().sw_status_error(int(word) & 0xFFFFFFFF)
+    if err == N.SW_ERR_TIMEOUT:
+        return DeviceWaitTimeout(f"{where}: a TMA-staged step block timed out (status word {word:#x})")
+    if err == N.SW_ERR_NONFINITE:
+        return Diverged(f"{where}: non-finite density (status word {word:#x})")
+    return None
 
 
 class WallSolver:
@@ -58,13 +75,13 @@ class WallSolver:
                       Lattice(self.grid, dtype, device=self.device).zero_()]   # f1 = zeros, lbm3d.py:294
         else:
             self.f = [Lattice(self.grid, dtype, device=self.device)]
-            from . import _native as N
             nb = N.lib().sw_aa_ghost_elems(self.grid.gp) * N.DTYPE_BYTES[self.f[0].dtype]
             self.ghost = torch.empty(int(nb), dtype=torch.uint8, device=self.device)
             if chunk % 2:
                 raise ValueError("the AA pattern replays graphs of an even number of steps")
         self.aa_odd_next = True      # AA: the next step is an odd one (the state is readable)
         self.cur = 0
+        self.status = StatusWord(device=self.device)   # divergence and time-out bits of every step
         self.force = ForceSeries(self.n_total, nz, device=self.device)
         self.acc = Accum(self.grid, device=self.device)
         self.t = 0
@@ -113,6 +130,7 @@ class WallSolver:
         self.uin.data.copy_(uin, non_blocking=True)
         self.force.data.zero_()
         self.acc.data.zero_()
+        self.status.clear()
         self.t, self.n_acc, self.cur = 0, 0, 0
         self.aa_odd_next = True
         return self
@@ -122,13 +140,13 @@ class WallSolver:
         storage type (stonewall.autotune); the state is not modified.  Returns (cfg, times)."""
         from . import autotune
         if self.pattern == "aa":
-            from . import _native as N
             return N.lib().sw_get_step_config(self.dtype), {}   # the in-place step has one configuration
         return autotune.tune(self, repeats=repeats)
 
     def init(self, noise=0.02, seed=7, noise_kind="uniform"):
-        """k_init on the current lattice (lbm3d.py:340)."""
+        """k_init on the current lattice (lbm3d.py:340); clears the status word."""
         K.k_init(self.state, self.flags, self.uin, noise, seed, noise_kind)
+        self.status.clear()
         return self
 
     # ------------------------------------------------------------ stepping
@@ -136,12 +154,13 @@ class WallSolver:
         g = self.grid
         if self.pattern == "aa":
             K.k_step_aa(self.f[0], self.aa_odd_next, self.flags, self.uin, self.nu0, self.cs, self.x_sponge,
-                        self.nu_sponge, force_rows, t_index, ghost=self.ghost, acc=self.acc if accumulate else None)
+                        self.nu_sponge, force_rows, t_index, ghost=self.ghost, acc=self.acc if accumulate else None,
+                        status=self.status)
             self.aa_odd_next = not self.aa_odd_next
             return
         src, dst = self.f[self.cur], self.f[1 - self.cur]
         K.k_step(src, dst, self.flags, self.uin, g.nx, g.ny, g.nz, self.nu0, self.cs, self.x_sponge,
-                 self.nu_sponge, force_rows, t_index, acc=self.acc if accumulate else None)
+                 self.nu_sponge, force_rows, t_index, acc=self.acc if accumulate else None, status=self.status)
         self.cur ^= 1
 
     def _accumulate_now(self, t):
@@ -178,8 +197,10 @@ class WallSolver:
         self._graphs[key] = (graph, n_acc)
         return self._graphs[key]
 
-    def advance(self, n, use_graphs=True):
-        """Run n steps (graph-replayed in chunks where possible)."""
+    def advance(self, n, use_graphs=True, check=True):
+        """Run n steps (graph-replayed in chunks where possible).  With check (the default) the status
+        word is read once at the end -- one wait for the queued steps -- and a diverged state or a
+        timed-out step raises Diverged / DeviceWaitTimeout; without, the steps stay queued."""
         n = min(int(n), self.n_total - self.t)
         c = self.chunk
         while n > 0:
@@ -198,7 +219,21 @@ class WallSolver:
             else:
                 self.step()
                 n -= 1
+        if check:
+            self.check_status()
         return self
+
+    def status_error(self):
+        """The failure recorded in the status word so far (Diverged / DeviceWaitTimeout), or None.
+        Reads the word: waits for the steps queued so far."""
+        return status_exception(self.status.read(), f"step {self.t}")
+
+    def check_status(self):
+        """Raise the failure recorded in the status word, if any."""
+        err = self.status_error()
+        if err is not None:
+            raise err
+        return True
 
     def run(self, check_every=5000, log=None):
         """Advance to n_total with a finiteness check every check_every steps (lbm3d.py:386-391)."""
@@ -361,6 +396,7 @@ class WallSolver:
         if info["sig"] != sig:
             raise ValueError(f"checkpoint {path} was made with different settings")
         self.t, self.n_acc = int(info["t"]), int(info["n_acc"])
+        self.status.clear()
         self.cur = 0
         self.aa_odd_next = True
         self.f[0].assign(np.load(os.path.join(path, "f.npy")))

@@ -33,6 +33,12 @@ int main(void) {
   CHECK(sw_step(&h, 9, (void *)16, (void *)32, (const uint8_t *)16, (const uint8_t *)16, (const float *)16, 1e-3,
                 0.1, 20, 0.05, NULL, 0, NULL) == SW_ERR_BAD_ARG);
   CHECK(sw_batch_graph_create(NULL) == SW_ERR_BAD_ARG);
+  /* a status word read back from the device maps to an error code */
+  CHECK(sw_status_error(0) == SW_OK);
+  CHECK(sw_status_error(SW_STATUS_NONFINITE) == SW_ERR_NONFINITE);
+  CHECK(sw_status_error(SW_STATUS_NONFINITE | SW_STATUS_TIMEOUT) == SW_ERR_TIMEOUT);
+  CHECK(sw_step_checked(&h, SW_F32, NULL, NULL, NULL, NULL, NULL, 1e-3, 0.1, 20, 0.05, NULL, 0, NULL, -1, NULL,
+                        NULL) == SW_ERR_BAD_ARG);
   printf("c abi ok: %s\n", sw_version());
   return 0;
 }

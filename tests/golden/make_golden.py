@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ by running the reference itself.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>   (or STONEWALL_REFERENCE=<path>)
 
 Needs the reference sources (stonewall3d/lbm3d.py, stonewall3d/geometry.py); the
 fixtures it writes are committed, so nothing else needs the sources.  lbm3d.py
@@ -121,10 +121,13 @@ def write_postprocess(out, driver_npz):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("STONEWALL_REFERENCE"),
+                    help="checkout of the reference repository (default: $STONEWALL_REFERENCE)")
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--only", default="", help="comma-separated fixture names to (re)write (default: all)")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give the reference checkout with --ref or STONEWALL_REFERENCE")
     lbm3d, geometry, wp = load_reference(a.ref)
     only = set(v for v in a.only.split(",") if v)
 

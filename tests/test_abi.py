@@ -65,6 +65,39 @@ def test_entry_points_reject_bad_arguments_before_launching(native_lib):
     assert L.sw_init(gp, 0, p, p, p, 0.02, 1, 7, None) == N.SW_ERR_BAD_ARG                       # noise kind
     assert L.sw_pack_f(gp, 0, 2, p, p, None) == N.SW_ERR_BAD_ARG                                  # ref dtype
     assert L.sw_force_to_f64(None, None, -1, None) == N.SW_ERR_BAD_ARG
+    q = ctypes.c_void_p(buf.ctypes.data + 32)
+    assert L.sw_step_checked(gp, 0, p, q, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None, -2, None,
+                             None) == N.SW_ERR_BAD_ARG                                           # cfg < -1
+    assert L.sw_step_checked(gp, 0, p, q, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None, 8, None,
+                             None) == N.SW_ERR_UNSUPPORTED                                       # TMA: 16-bit only
+    assert L.sw_step_checked(gp, 0, p, q, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None, -1,
+                             ctypes.c_void_p(buf.ctypes.data + 2), None) == N.SW_ERR_BAD_ARG     # status misaligned
+    assert L.sw_step_cfg(gp, 0, p, q, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None, -1, None) == N.SW_ERR_BAD_ARG
+
+
+def test_status_words_map_to_errors(native_lib):
+    """sw_status_error: the time-out bit wins (the timed-out cells were not written), then divergence."""
+    from stonewall import _native as N
+    L = native_lib
+    assert L.sw_status_error(0) == N.SW_OK
+    assert L.sw_status_error(N.SW_STATUS_NONFINITE) == N.SW_ERR_NONFINITE
+    assert L.sw_status_error(N.SW_STATUS_TIMEOUT) == N.SW_ERR_TIMEOUT
+    assert L.sw_status_error(N.SW_STATUS_TIMEOUT | N.SW_STATUS_NONFINITE) == N.SW_ERR_TIMEOUT
+    assert L.sw_status_error(0x80) == N.SW_OK                                # bits nobody sets
+    from stonewall.solver import DeviceWaitTimeout, Diverged, status_exception
+    assert status_exception(0, "x") is None
+    assert isinstance(status_exception(1, "x"), Diverged)
+    assert isinstance(status_exception(3, "x"), DeviceWaitTimeout)
+
+
+def test_tma_poll_limit_hook_reads_and_restores(native_lib):
+    L = native_lib
+    old = L.sw_debug_tma_poll_limit(-1)                 # read only
+    assert old == 1 << 14
+    assert L.sw_debug_tma_poll_limit(0) == old
+    assert L.sw_debug_tma_poll_limit(-1) == 0
+    assert L.sw_debug_tma_poll_limit(old) == 0
+    assert L.sw_debug_tma_poll_limit(-1) == old
 
 
 def test_native_unavailable_is_loud(monkeypatch, tmp_path):

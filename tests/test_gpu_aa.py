@@ -141,7 +141,7 @@ def test_aa_abi_rejects_bad_arguments(cuda):
     ghost = torch.empty(N.lib().sw_aa_ghost_elems(g.gp) * 4, dtype=torch.uint8, device="cuda")
     L = N.lib()
     args = lambda odd, gh: (g.gp, f.dtype, f.ptr, odd, fl.ptr, fl.tiles_ptr, uv.ptr, 2e-3, 0.1, 32, 0.05,
-                            None, 0, None, gh, None)
+                            None, 0, None, gh, None, None)
     assert L.sw_step_aa(*args(2, ghost.data_ptr())) == N.SW_ERR_BAD_ARG
     assert L.sw_step_aa(*args(-1, ghost.data_ptr())) == N.SW_ERR_BAD_ARG
     assert L.sw_step_aa(*args(1, None)) == N.SW_ERR_BAD_ARG
