@@ -507,9 +507,11 @@ template <> struct Pack16<SW_BF16_SHIFT> {
 // half lands in the row's padding columns (x >= nx), which nothing reads.  The
 // inlet cell (x0 == 0, lbm3d.py:67-71) is collided like the others and then
 // overwritten by its equilibrium in a branch only its lane takes.
-template <int DT, bool ACC, typename Ctx>
+// acc_old(k): the old float64 sums of the pair for sum k (a double2; .y unused
+// when x0 + 1 is past the row end), called where they are added.
+template <int DT, bool ACC, typename Ctx, typename AccOld>
 __device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q], int x0, int c, int z, bool inlet,
-                                                   const double2 (&acc_old)[4]) {
+                                                   AccOld &&acc_old) {
   using S = Store<DT>;
   using T = typename S::T;
   using PK = Pack16<DT>;
@@ -539,16 +541,16 @@ __device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q
     const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
     const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
     if (has_b) {                                        // cells x0, x0 + 1: one 16-byte update per sum
-      const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
+      const double2 v0 = acc_old(0), v1 = acc_old(1), v2 = acc_old(2), v3 = acc_old(3);
       __stcs(reinterpret_cast<double2 *>(p.accp(0) + c), make_double2(v0.x + ra, v0.y + (double)rho.v.y));
       __stcs(reinterpret_cast<double2 *>(p.accp(1) + c), make_double2(v1.x + xa, v1.y + (double)ux.v.y));
       __stcs(reinterpret_cast<double2 *>(p.accp(2) + c), make_double2(v2.x + ya, v2.y + (double)uy.v.y));
       __stcs(reinterpret_cast<double2 *>(p.accp(3) + c), make_double2(v3.x + za, v3.y + (double)uz.v.y));
     } else {
-      __stcs(p.accp(0) + c, acc_old[0].x + ra);
-      __stcs(p.accp(1) + c, acc_old[1].x + xa);
-      __stcs(p.accp(2) + c, acc_old[2].x + ya);
-      __stcs(p.accp(3) + c, acc_old[3].x + za);
+      __stcs(p.accp(0) + c, acc_old(0).x + ra);
+      __stcs(p.accp(1) + c, acc_old(1).x + xa);
+      __stcs(p.accp(2) + c, acc_old(2).x + ya);
+      __stcs(p.accp(3) + c, acc_old(3).x + za);
     }
   }
 }
@@ -609,7 +611,7 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
     }
   });
   if (!live) return;
-  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, acc_old);
+  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, [&](int k) { return acc_old[k]; });
 }
 
 // One warp, the row segments 2 bx and 2 bx + 1 of (y, z).

@@ -47,6 +47,9 @@ constexpr int kTmaBoxBytes = kTmaRowBytes * 4;               // one population, 
 constexpr int kTmaWrapBytes = 256;                           // one-row box (160 B) in a 128-aligned slot
 constexpr int kTmaWrapSlots = 10;                            // the populations with c_y != 0
 constexpr int kTmaStageBytes = Q * kTmaBoxBytes + kTmaWrapSlots * kTmaWrapBytes;
+// accumulating steps also stage the float64 sums of the item: 64 cells x 4 rows x 4 sums
+constexpr int kTmaAccBytes = 64 * 4 * 4 * 8;
+template <bool ACC> constexpr int tma_stage_bytes() { return kTmaStageBytes + (ACC ? kTmaAccBytes : 0); }
 
 // wrap slot of a population with c_y != 0 (3, 4, 7, 8, 9, 10, 15, 16, 17, 18)
 __host__ __device__ constexpr int wrap_slot(int i) {
@@ -104,13 +107,15 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map
 }
 
 
-// Issue the copies of item (x0, y0, z) into stage `st`, arriving on `bar` (one thread).
-__device__ __forceinline__ void tma_issue(const CUtensorMap *map, const CUtensorMap *map1, const Geom &g, int x0,
-                                          int y0, int z, uint32_t st, uint32_t bar) {
+// Issue the copies of item (x0, y0, z) into stage `st`, arriving on `bar` (one
+// thread); with ACC also the item's float64 sums (map_acc) behind the boxes.
+template <bool ACC>
+__device__ __forceinline__ void tma_issue(const CUtensorMap *map, const CUtensorMap *map1, const CUtensorMap *map_acc,
+                                          const Geom &g, int x0, int y0, int z, uint32_t st, uint32_t bar) {
   const bool top = z == g.nz - 1;
   const bool wrap_lo = y0 == 0;                  // source row -1 of the first warp (c_y = +1)
   const bool wrap_hi = y0 + 4 >= g.ny;           // source row ny of the warp at y = ny - 1 (c_y = -1)
-  uint32_t bytes = Q * kTmaBoxBytes;
+  uint32_t bytes = Q * kTmaBoxBytes + (ACC ? kTmaAccBytes : 0);
   if (wrap_lo) bytes += 5 * kTmaRowBytes;
   if (wrap_hi) bytes += 5 * kTmaRowBytes;
   mbar_expect_tx(bar, bytes);
@@ -126,6 +131,7 @@ __device__ __forceinline__ void tma_issue(const CUtensorMap *map, const CUtensor
       if (wrap_hi) tma_load_4d(st + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes, map1, x0 - 8, 0, zl, pop, bar);
     }
   });
+  if constexpr (ACC) tma_load_4d(st + kTmaStageBytes, map_acc, x0, y0, z, 0, bar);
 }
 
 // The pair-kernel fast path with the sources read from the staged boxes (st: the stage).
@@ -163,23 +169,18 @@ __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t
       v[i] = F2(has_b ? o.y : o.x, has_r ? PK::lo(right) : o.y);
     }
   });
-  double2 acc_old[4];
-  if (ACC && live) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (has_b) acc_old[k] = __ldcs(reinterpret_cast<const double2 *>(p.accp(k) + c));
-      else acc_old[k] = make_double2(__ldcs(p.accp(k) + c), 0.0);
-    }
-  }
   if (!live) return;
-  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, acc_old);
+  // accumulating steps: the pair's old sums from the staged box [4 sums][4 rows][64 cells], read where added
+  const double2 *acc_box = reinterpret_cast<const double2 *>(st + kTmaStageBytes) + w * 32 + lane;
+  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, [&](int k) { return acc_box[k * 4 * 32]; });
 }
 
 // Grid: (ceil(pitch / 64), ceil(ceil(ny / 4) / ITEMS), nz); block = 4 warps, warp w = row y0 + w.
 template <int DT, bool ACC, typename Cfg>
 __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     k_step_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap map1,
-               const __grid_constant__ StepParams p) {
+               const __grid_constant__ CUtensorMap map_acc, const __grid_constant__ StepParams p) {
+  constexpr int kStage = tma_stage_bytes<ACC>();
   static_assert(2 * Cfg::ITEMS <= 32, "one lane per tile byte of the block's items");
   extern __shared__ __align__(128) uint8_t smem_raw[];
   __shared__ __align__(8) unsigned long long bars[Cfg::NSTAGE];
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     for (int j = 0; j < Cfg::NSTAGE && j < n_items; ++j)
-      tma_issue(&map, &map1, g, x0s, (yb0 + j) * 4, z, base + j * kTmaStageBytes, smem_u32(&bars[j]));
+      tma_issue<ACC>(&map, &map1, &map_acc, g, x0s, (yb0 + j) * 4, z, base + j * kStage, smem_u32(&bars[j]));
   }
   // The segment classes of this warp's rows in all its items, fetched once up
   // front (lane j: segment 2 bx of item j, lane ITEMS + j: segment 2 bx + 1),
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
   int j = 0;
   for (; j < n_items; ++j) {
     const int s = j % Cfg::NSTAGE;
-    const uint32_t st = base + s * kTmaStageBytes;
+    const uint32_t st = base + s * kStage;
     const int y = (yb0 + j) * 4 + w;
     const uint8_t ka = (uint8_t)__shfl_sync(0xffffffffu, kinds, j);
     const uint8_t kb = (uint8_t)__shfl_sync(0xffffffffu, kinds, Cfg::ITEMS + j);
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     if (ok && y < g.ny && !(ka & kb & TILE_ALL_SOLID)) {
       const int x0 = x0s + 2 * lane;
       if (!((ka | kb) & TILE_CHECK)) {
-        tma_pair_fast<DT, ACC>(p, smem + s * kTmaStageBytes, x0, y, z, w, lane);
+        tma_pair_fast<DT, ACC>(p, smem + s * kStage, x0, y, z, w, lane);
       } else {                                                        // next to stones / ground: per cell
         float fxw = 0.0f, fzw = 0.0f;
         int hit = 0;
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     ok = __syncthreads_and(ok);                                       // stage s is free again
     if (!ok) break;
     if (leader && j + Cfg::NSTAGE < n_items)
-      tma_issue(&map, &map1, g, x0s, (yb0 + j + Cfg::NSTAGE) * 4, z, st, smem_u32(&bars[s]));
+      tma_issue<ACC>(&map, &map1, &map_acc, g, x0s, (yb0 + j + Cfg::NSTAGE) * 4, z, st, smem_u32(&bars[s]));
   }
   if (!ok && leader) {                                                // item j failed: items j .. j+NSTAGE-1
     atomicAdd(&g_tma_timeouts, 1u);                                   // were issued; let their copies land
@@ -273,16 +274,34 @@ inline bool encode_lattice_map(CUtensorMap *m, const void *f, const Geom &g, int
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The float64 sums acc ([4][nz][ny][pitch]) as a 4-D tensor, boxes of 64 cells x 4 rows x 1 level x 4 sums.
+inline bool encode_acc_map(CUtensorMap *m, const double *acc, const Geom &g) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dim[4] = {(cuuint64_t)g.pitch, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 4};
+  const cuuint64_t stride[3] = {(cuuint64_t)g.pitch * 8, (cuuint64_t)g.pitch * g.ny * 8, (cuuint64_t)g.plane * 8};
+  const cuuint32_t box[4] = {64, 4, 1, 4};
+  const cuuint32_t estride[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<double *>(acc), dim, stride, box, estride,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int DT, bool ACC, typename Cfg>
 cudaError_t launch_tma(const StepParams &p, cudaStream_t s) {
-  CUtensorMap map, map1;
+  CUtensorMap map, map1, map_acc;
   if (!encode_lattice_map(&map, p.fin, p.g, 4) || !encode_lattice_map(&map1, p.fin, p.g, 1))
     return cudaErrorNotSupported;
-  const int smem = Cfg::NSTAGE * kTmaStageBytes + 128;               // + alignment slack; <= 48 KB
-  static_assert(Cfg::NSTAGE * kTmaStageBytes + 128 <= 48 * 1024, "stages exceed the default shared memory");
+  if (ACC) {
+    if (!encode_acc_map(&map_acc, p.acc, p.g)) return cudaErrorNotSupported;
+  } else {
+    map_acc = map;                                                   // not read
+  }
+  constexpr int smem = Cfg::NSTAGE * tma_stage_bytes<ACC>() + 128;   // + alignment slack; <= 48 KB
+  static_assert(smem <= 48 * 1024, "stages exceed the default shared memory");
   const int nyb = (p.g.ny + 3) / 4;
   const dim3 grid((unsigned)((p.g.nseg_x + 1) / 2), (unsigned)((nyb + Cfg::ITEMS - 1) / Cfg::ITEMS), (unsigned)p.g.nz);
-  k_step_tma<DT, ACC, Cfg><<<grid, dim3(32, 4), smem, s>>>(map, map1, p);
+  k_step_tma<DT, ACC, Cfg><<<grid, dim3(32, 4), smem, s>>>(map, map1, map_acc, p);
   return cudaGetLastError();
 }
 

@@ -195,3 +195,31 @@ def test_short_horizon_cd_against_float64(cuda):
     assert out["f16"]["mean"] < 0.01 and out["f16"]["peak"] < 0.01
     assert out["f32"]["mean"] < 1e-3 and out["f32"]["peak"] < 1e-3
     assert np.isfinite([out["bf16"]["mean"], out["bf16"]["peak"]]).all()
+
+
+@pytest.mark.parametrize("cfg", [0, 4, 8])
+@pytest.mark.parametrize("dtype", ["f16", "bf16"])
+def test_16bit_accumulating_step_sums_match_oracle(dtype, cfg, cuda, oracle_mod):
+    """The fused accumulation (k_macro + k_accum of lbm3d.py:367-369 in the step) in 16-bit storage,
+    one cell per thread (0), two (4) and with the sums staged by TMA (8): the sums are formed from
+    the pulled populations, which the storage format holds exactly, so they meet the float64
+    oracle's macro field of the new state to float32 rounding (the collision conserves rho and m)."""
+    from stonewall.fields import Accum, Flags, ForceSeries, Grid, Lattice, StatusWord
+    from stonewall.kernels import DeviceVector, k_step
+    for case in [(64, 32, 33, 1), (45, 7, 10, 2), "step_edge"]:
+        flag, uin, f0, args = _case(case, oracle_mod)
+        f0q = representable(f0, flag, dtype)
+        nx, ny, nz = flag.shape
+        g = Grid(nx, ny, nz)
+        flags, uv = Flags(g, flag), DeviceVector(uin)
+        src, dst = Lattice(g, dtype).assign(f0q), Lattice(g, dtype).zero_()
+        acc, status = Accum(g), StatusWord()
+        nu0, cs, xs, nus = args
+        k_step(src, dst, flags, uv, nx, ny, nz, nu0, cs, xs, nus, ForceSeries(1, nz), 0, acc=acc, status=status,
+               cfg=cfg)
+        assert status.read() == 0
+        want, _ = oracle_mod.run(f0q, flag, uin.astype(np.float64), nu0, cs, xs, 1, nus)
+        u = oracle_mod.macro(want, flag)                          # float64 (rho, ux, uy, uz), solids (1, 0, 0, 0)
+        got = acc.numpy(solid=flag != 0, n_acc=1)
+        np.testing.assert_allclose(got[0], u[0], rtol=2e-6, atol=0)
+        np.testing.assert_allclose(got[1:], u[1:], rtol=0, atol=2e-6 * np.abs(u[1:]).max())
