@@ -224,9 +224,12 @@ template <int WY_, int MINB_> struct StepCfg {
 // two cells per thread (16-bit storage only), see k_step_pair
 #define SW_PAIR_CONFIGS(X) X(4, 4, 8) X(5, 4, 10) X(6, 8, 4) X(7, 8, 5)
 // two cells per thread with TMA-staged sources (16-bit storage only), see sw_tma.cuh:
-// (id, row-groups per block, stages, resident blocks)
-#define SW_TMA_CONFIGS(X) X(8, 4, 2, 8) X(9, 2, 2, 8) X(10, 4, 2, 10)
-constexpr int kStepConfigs = 11;
+// (id, row-groups per block, stages, resident blocks asked of the register allocator).
+// Shared memory holds a 2-stage block to 7 resident blocks (4 on accumulating
+// steps), so 11-13 give the registers that residency leaves (72 and 128 per thread).
+#define SW_TMA_CONFIGS(X) X(8, 4, 2, 8) X(9, 2, 2, 8) X(10, 4, 2, 10) X(11, 4, 2, 7) X(12, 2, 2, 7) X(13, 4, 2, 4) \
+  X(14, 4, 3, 5)
+constexpr int kStepConfigs = 15;
 
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
 // tests (segments next to stones, the ground or a fluid cell at z = 0).
@@ -507,17 +510,18 @@ template <> struct Pack16<SW_BF16_SHIFT> {
 // half lands in the row's padding columns (x >= nx), which nothing reads.  The
 // inlet cell (x0 == 0, lbm3d.py:67-71) is collided like the others and then
 // overwritten by its equilibrium in a branch only its lane takes.
-// acc_old(k): the old float64 sums of the pair for sum k (a double2; .y unused
-// when x0 + 1 is past the row end), called where they are added.
+// has_b: cell x0 + 1 exists (x0 + 1 < nx).  acc_old(k): the old float64 sums
+// of the pair for sum k (a double2; .y unused without has_b), called where
+// they are added.
 template <int DT, bool ACC, typename Ctx, typename AccOld>
 __device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q], int x0, int c, int z, bool inlet,
-                                                   AccOld &&acc_old) {
+                                                   bool has_b, AccOld &&acc_old) {
   using S = Store<DT>;
   using T = typename S::T;
   using PK = Pack16<DT>;
   const Phys<float> ph = phys<float>(p);
   f2 rho, ux, uy, uz;
-  collide2(v, x0, x0 + 1 < p.g.nx, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz,
+  collide2(v, x0, has_b, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz,
            p.status, [&](auto I, f2 o) {
              constexpr int i = decltype(I)::value;
              __stcs(reinterpret_cast<unsigned int *>(p.template out<T>(i) + c), PK::pack(o.v.x, o.v.y));
@@ -537,7 +541,6 @@ __device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q
     });
   }
   if (ACC) {
-    const bool has_b = x0 + 1 < p.g.nx;
     const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
     const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
     if (has_b) {                                        // cells x0, x0 + 1: one 16-byte update per sum
@@ -611,7 +614,7 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
     }
   });
   if (!live) return;
-  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, [&](int k) { return acc_old[k]; });
+  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_old[k]; });
 }
 
 // One warp, the row segments 2 bx and 2 bx + 1 of (y, z).

@@ -135,15 +135,18 @@ __device__ __forceinline__ void tma_issue(const CUtensorMap *map, const CUtensor
 }
 
 // The pair-kernel fast path with the sources read from the staged boxes (st: the stage).
-template <int DT, bool ACC>
+// INTERIOR: the warp's row is neither the inlet segment pair nor the last one
+// (every lane's cells and right neighbour exist) nor a periodic edge row in y,
+// so no lane needs the inlet, outlet or wrap selects (decided per warp and item).
+template <int DT, bool ACC, bool INTERIOR>
 __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t *st, int x0, int y, int z, int w,
                                               int lane) {
   using PK = Pack16<DT>;
   const Geom &g = p.g;
-  const bool live = x0 < g.nx;
-  const bool has_b = x0 + 1 < g.nx;
-  const bool has_r = x0 + 2 < g.nx;
-  const bool inlet = x0 == 0;
+  const bool live = INTERIOR || x0 < g.nx;
+  const bool has_b = INTERIOR || x0 + 1 < g.nx;
+  const bool has_r = INTERIOR || x0 + 2 < g.nx;
+  const bool inlet = !INTERIOR && x0 == 0;
   const int c = (z * g.ny + y) * g.pitch + x0;
   const int lane_word = 4 + lane;                                     // 32-bit word of elements 8 + 2 lane, + 1
   f2 v[Q];
@@ -151,9 +154,9 @@ __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t
     constexpr int i = decltype(I)::value;
     constexpr int ex = CX(i), ey = CY(i);
     const uint8_t *rowp = st + i * kTmaBoxBytes + w * kTmaRowBytes;
-    if constexpr (ey == 1) {
+    if constexpr (ey == 1 && !INTERIOR) {
       if (y == 0) rowp = st + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes;
-    } else if constexpr (ey == -1) {
+    } else if constexpr (ey == -1 && !INTERIOR) {
       if (y == g.ny - 1) rowp = st + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes;
     }
     const uint32_t *row = reinterpret_cast<const uint32_t *>(rowp);
@@ -172,7 +175,7 @@ __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t
   if (!live) return;
   // accumulating steps: the pair's old sums from the staged box [4 sums][4 rows][64 cells], read where added
   const double2 *acc_box = reinterpret_cast<const double2 *>(st + kTmaStageBytes) + w * 32 + lane;
-  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, [&](int k) { return acc_box[k * 4 * 32]; });
+  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_box[k * 4 * 32]; });
 }
 
 // Grid: (ceil(pitch / 64), ceil(ceil(ny / 4) / ITEMS), nz); block = 4 warps, warp w = row y0 + w.
@@ -226,7 +229,10 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     if (ok && y < g.ny && !(ka & kb & TILE_ALL_SOLID)) {
       const int x0 = x0s + 2 * lane;
       if (!((ka | kb) & TILE_CHECK)) {
-        tma_pair_fast<DT, ACC>(p, smem + s * kStage, x0, y, z, w, lane);
+        if (x0s > 0 && x0s + 2 * SEG < g.nx && y > 0 && y < g.ny - 1)     // uniform across the warp
+          tma_pair_fast<DT, ACC, true>(p, smem + s * kStage, x0, y, z, w, lane);
+        else
+          tma_pair_fast<DT, ACC, false>(p, smem + s * kStage, x0, y, z, w, lane);
       } else {                                                        // next to stones / ground: per cell
         float fxw = 0.0f, fzw = 0.0f;
         int hit = 0;
@@ -297,8 +303,17 @@ cudaError_t launch_tma(const StepParams &p, cudaStream_t s) {
   } else {
     map_acc = map;                                                   // not read
   }
-  constexpr int smem = Cfg::NSTAGE * tma_stage_bytes<ACC>() + 128;   // + alignment slack; <= 48 KB
-  static_assert(smem <= 48 * 1024, "stages exceed the default shared memory");
+  constexpr int smem = Cfg::NSTAGE * tma_stage_bytes<ACC>() + 128;   // + alignment slack
+  static_assert(smem <= 227 * 1024, "stages exceed the shared memory of a block");
+  if constexpr (smem > 48 * 1024) {                                  // beyond the default: opt in, once
+    static bool opted = false;
+    if (!opted) {
+      const cudaError_t e = cudaFuncSetAttribute(k_step_tma<DT, ACC, Cfg>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 smem);
+      if (e != cudaSuccess) return e;
+      opted = true;
+    }
+  }
   const int nyb = (p.g.ny + 3) / 4;
   const dim3 grid((unsigned)((p.g.nseg_x + 1) / 2), (unsigned)((nyb + Cfg::ITEMS - 1) / Cfg::ITEMS), (unsigned)p.g.nz);
   k_step_tma<DT, ACC, Cfg><<<grid, dim3(32, 4), smem, s>>>(map, map1, map_acc, p);

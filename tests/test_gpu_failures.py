@@ -104,7 +104,7 @@ def test_tma_timeout_is_reported_and_the_context_stays_usable(cuda):
     assert word & N.SW_STATUS_TIMEOUT
     assert L.sw_status_error(word) == N.SW_ERR_TIMEOUT
     assert blocks > 0
-    assert set(times) == set(range(8))                   # the TMA-staged configurations 8-10 were left out
+    assert set(times) == set(range(8))                   # the TMA-staged configurations (8 and up) were left out
     word2, again = _one_step(flag, uin, f0, "f16", 8)
     assert word2 == 0 and L.sw_tma_timeouts() == 0
     np.testing.assert_array_equal(again.numpy(np.float64), ref.numpy(np.float64))
