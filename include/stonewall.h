@@ -242,6 +242,11 @@ typedef struct sw_batch_header {
   int32_t n;             /* entries in the table */
   int32_t reserved;
   int64_t total_items;   /* sum of items (set by sw_batch_prepare) */
+  /* work counters of a launch: zero before it (sw_batch_prepare sets them), used by the
+   * kernel's blocks to take items in order, and zero again when the launch ends */
+  uint64_t next_item;
+  uint32_t done_blocks;
+  uint32_t reserved2;
 } sw_batch_header;
 
 /* Host only: check entries[0..n) for storage type dtype and configuration cfg

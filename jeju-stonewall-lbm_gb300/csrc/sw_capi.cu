@@ -288,6 +288,9 @@ int sw_batch_prepare(sw_batch_entry *entries, int32_t n, int dtype, int cfg, sw_
   hdr->n = n;
   hdr->reserved = 0;
   hdr->total_items = item0;
+  hdr->next_item = 0;
+  hdr->done_blocks = 0;
+  hdr->reserved2 = 0;
   return SW_OK;
 }
 

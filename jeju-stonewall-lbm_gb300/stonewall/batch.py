@@ -41,7 +41,8 @@ class SwBatchEntry(ctypes.Structure):
 
 
 class SwBatchHeader(ctypes.Structure):
-    _fields_ = [("n", ctypes.c_int32), ("reserved", ctypes.c_int32), ("total_items", ctypes.c_int64)]
+    _fields_ = [("n", ctypes.c_int32), ("reserved", ctypes.c_int32), ("total_items", ctypes.c_int64),
+                ("next_item", ctypes.c_uint64), ("done_blocks", ctypes.c_uint32), ("reserved2", ctypes.c_uint32)]
 
 
 def _bind():
