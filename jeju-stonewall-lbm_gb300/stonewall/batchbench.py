@@ -1,10 +1,12 @@
 """Many-wall batch run: aggregate throughput and per-wall accuracy against the plain form.
 
     python -m stonewall.batchbench [--walls 64] [--steps 10000] [--dtype f16] [--no-plain]
+                                   [--H 40] [--porosity 0.2] [--seed 0] [--mode persistent --cfg 4]
 
 Walls: for i in 0..walls-1, rng = default_rng(i) draws H from {16, 24, 32, 40}
-and porosity from U[0, 0.5]; each wall is an ellipsoid-packed stone wall with
-seed i in a 20H x 4H x 4H domain (stonewall.params.baseline_params).  All walls
+and porosity from U[0, 0.5] (--H / --porosity fix them for every wall); each
+wall is an ellipsoid-packed stone wall with seed seed + i in a 20H x 4H x 4H
+domain (stonewall.params.baseline_params).  All walls
 advance together in one persistent launch per step (stonewall.batch.Batch),
 replayed from a captured CUDA graph, or as one graph of per-wall launches
 per chunk (the autotuner picks the faster mode).  The plain form is the same walls solved
@@ -27,13 +29,14 @@ from .params import baseline_params, flags_from_wall
 from .solver import WallSolver
 
 
-def wall_specs(n):
+def wall_specs(n, H=None, porosity=None, seed=0):
     out = []
     for i in range(n):
         rng = np.random.default_rng(i)
-        H = int(rng.choice([16, 24, 32, 40]))
-        porosity = float(rng.uniform(0.0, 0.5))
-        out.append(dict(i=i, H=H, porosity=porosity, seed=i))
+        h = int(rng.choice([16, 24, 32, 40]))
+        por = float(rng.uniform(0.0, 0.5))
+        out.append(dict(i=i, H=h if H is None else int(H), porosity=por if porosity is None else float(porosity),
+                        seed=seed + i))
     return out
 
 
@@ -65,14 +68,24 @@ def main(argv=None):
     ap.add_argument("--no-plain", action="store_true", help="skip the float32 one-wall-at-a-time reference")
     ap.add_argument("--mode", default="auto", choices=["auto", "persistent", "graph"],
                     help="batch mode (auto: the autotuner times both)")
+    ap.add_argument("--H", type=int, default=None, help="wall height of every wall (default: drawn per wall)")
+    ap.add_argument("--porosity", type=float, default=None, help="porosity of every wall (default: drawn)")
+    ap.add_argument("--seed", type=int, default=0, help="mask seed of wall 0 (wall i: seed + i)")
+    ap.add_argument("--cfg", type=int, default=None,
+                    help="persistent kernel launch configuration (with --mode persistent; skips the autotuner)")
     a = ap.parse_args(argv)
-    specs = wall_specs(a.walls)
+    if a.cfg is not None and a.mode != "persistent":
+        ap.error("--cfg selects a configuration of the persistent kernel: give --mode persistent")
+    specs = wall_specs(a.walls, a.H, a.porosity, a.seed)
     t_build = time.time()
     batch = Batch(dtype=a.dtype, chunk=a.chunk, max_members=max(64, a.walls))
     members = [batch.add(make_solver(sp, a.steps, a.dtype)) for sp in specs]
     t_build = time.time() - t_build
     modes = ("persistent", "graph") if a.mode == "auto" else (a.mode,)
-    cfg, cfg_times = batch.autotune(modes=modes)
+    if a.cfg is None:
+        cfg, cfg_times = batch.autotune(modes=modes)
+    else:
+        batch.cfg, batch.mode, cfg_times = a.cfg, "persistent", {}
     cells = batch.cells()
     torch.cuda.synchronize()
     t0 = time.time()
