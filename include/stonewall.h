@@ -286,6 +286,61 @@ int64_t sw_batch_graph_launches(const sw_batch_graph *g);
 /* force rows (fixed point) -> double, n values. */
 int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s);
 
+/* ---------------------------------------------------------------- wall loads on the device
+ * The coefficient series of lbm3d.py:396-407 from the fixed-point force rows
+ * force[n_steps][nz][2] (16-byte aligned): coef[0][t] = Cd = Fx / (q A),
+ * coef[1][t] = Cl = Fz / (q A), coef[2][t] = Cm = M / (q A H), with Fx, Fz the
+ * sums over the levels, M = sum_z F_x(z) (z - 1/2), q A = U_H^2 / 2 * H ny;
+ * coef is [3][n_steps] doubles. */
+int sw_coefficients(const int64_t *force, int64_t n_steps, int32_t nz, double UH, double H, int32_t ny, double *coef,
+                    sw_stream s);
+/* postprocess.py:65-82 on the device: over the steps t >= n_spin of a coefficient
+ * series from sw_coefficients, stats[0..5] = mean Cd, max Cd, std Cd (about the
+ * mean), mean Cm, max Cm, mean Cl (6 doubles, device memory; NaN with no step
+ * left).  A solve's statistics then need 48 bytes downloaded, not its force series. */
+int sw_coef_stats(const double *coef, int64_t n_steps, int64_t n_spin, double *stats, sw_stream s);
+
+/* ---------------------------------------------------------------- wall masks on the device
+ * The per-cell work of the two stone-wall generators of the Python package
+ * (stonewall/geometry.py); their random draws stay on the host, so a seed gives
+ * the host generator's mask bit for bit.
+ *
+ * Ellipsoid packer (the BASELINE wall; no reference counterpart): candidate
+ * stones drawn on the host in the generator's order, each with its cell range
+ * x in [x0, x1), y in [y0, y1) (periodic, unwrapped), k in [k0, k1).  Cell
+ * (x, y, k) is inside when, with a = (x + 1/2, y + 1/2, k - 1/2) - centre,
+ * t_j = ((a_0 rot[j] + a_1 rot[3 + j]) + a_2 rot[6 + j]) / semi[j] and
+ * (t_0^2 + t_1^2) + t_2^2 <= 1 (float64, in that order, no contraction). */
+typedef struct sw_ellipsoid {
+  double centre[3];
+  double semi[3];
+  double rot[9];                 /* rotation, row-major */
+  int32_t x0, x1, y0, y1, k0, k1;
+} sw_ellipsoid;
+/* Bytes of the bitset of the wall box x in [X0, X0 + T), y in [0, ny),
+ * k in [1, z_hi): bit ((x - X0) ny + y) (z_hi - 1) + (k - 1); -1 on bad sizes. */
+int64_t sw_pack_box_bytes(int32_t T, int32_t ny, int32_t z_hi);
+/* The packer's loop over cand[0..n) (device memory) in order, one block on s:
+ * while state[0] (solid cells so far) < target - 1/2, count the cells the
+ * candidate adds; accept it unless it adds none or state[0] + n_new > target
+ * + n_new / 2; set its cells in box_bits (device, in/out).  state[1] receives
+ * the candidates consumed.  Boxes above 200 KiB of bits: SW_ERR_TOO_LARGE. */
+int sw_pack_ellipsoids(const sw_ellipsoid *cand, int32_t n, int32_t X0, int32_t T, int32_t ny, int32_t z_hi,
+                       double target, uint32_t *box_bits, int64_t *state, sw_stream s);
+/* Course-wall rasteriser, geometry.py:68-84: stone s (device array) marks cell
+ * (x, y mod ny, k) of mask[nx][ny][nz] (device, uint8, reference layout; ORed
+ * in) when (|x + 1/2 - xc| / a)^p + (|y + 1/2 - yc| / b)^p + (|k - 1/2 - zc| /
+ * c)^p <= 1.  Cells whose sum is within 1e-12 of 1, where this GPU's pow and
+ * the host's may round apart, are not decided: they are listed in amb
+ * (device, 1 + 4 cap ints: count, then (stone, x, y, k) per cell) for the
+ * host to decide with its own arithmetic. */
+typedef struct sw_stone {
+  double xc, yc, zc, a, b, c, p;
+  int32_t x0, x1, y0, y1, k0, k1;
+} sw_stone;
+int sw_voxelize_stones(const sw_stone *stones, int32_t n, int32_t nx, int32_t ny, int32_t nz, uint8_t *mask,
+                       int32_t *amb, int32_t cap, sw_stream s);
+
 /* ---------------------------------------------------------------- viewer payload
  * From the macro field u of sw_macro (device layout [4][nz][ny][pitch]).
  * k_slice_xz, lbm3d.py:191-194 (lbm3d.py:372): out[4][nx][nz] = u at y = y0.

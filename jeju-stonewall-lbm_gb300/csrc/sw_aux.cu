@@ -315,6 +315,116 @@ cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cuda
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- wall-load coefficients
+// lbm3d.py:396-407: per step t, Fx = sum_z F_x(z), Fz = sum_z F_z(z) and the
+// overturning moment M = sum_z F_x(z) (z - 1/2) about the wall base, as
+// Cd = Fx / (q A), Cl = Fz / (q A), Cm = M / (q A H), q A = U_H^2 / 2 * H ny.
+// One warp per step: lanes over the levels (coalesced 16-byte rows), float64
+// partial sums combined by an xor butterfly in a fixed order.
+__global__ void k_coefficients(const long long *force, long long n_steps, int nz, double qa, double H,
+                               double *coef) {
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= n_steps) return;                                  // uniform across the warp
+  const longlong2 *row = reinterpret_cast<const longlong2 *>(force + t * 2 * nz);
+  double fx = 0.0, fz = 0.0, m = 0.0;
+  for (int z = lane; z < nz; z += 32) {
+    const longlong2 v = row[z];
+    const double x = (double)v.x * (1.0 / FORCE_SCALE), y = (double)v.y * (1.0 / FORCE_SCALE);
+    fx += x;
+    fz += y;
+    m += x * ((double)z - 0.5);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+    m += __shfl_xor_sync(0xffffffffu, m, o);
+  }
+  if (lane == 0) {
+    coef[t] = fx / qa;
+    coef[n_steps + t] = fz / qa;
+    coef[2 * n_steps + t] = m / (qa * H);
+  }
+}
+
+// postprocess.py:65-82 over the steps t >= n_spin of the coefficient series:
+// stats = mean Cd, max Cd, std Cd (about the mean, two passes), mean Cm, max Cm,
+// mean Cl; NaN when no step is left.  One block; fixed reduction order.
+constexpr int kStatThreads = 512;
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  const int tid = threadIdx.x;
+  sh[tid] = v;
+  __syncthreads();
+  for (int s = kStatThreads / 2; s > 0; s >>= 1) {
+    if (tid < s) sh[tid] += sh[tid + s];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+__device__ __forceinline__ double block_max(double v, double *sh) {
+  const int tid = threadIdx.x;
+  sh[tid] = v;
+  __syncthreads();
+  for (int s = kStatThreads / 2; s > 0; s >>= 1) {
+    if (tid < s) sh[tid] = fmax(sh[tid], sh[tid + s]);
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+__global__ void __launch_bounds__(kStatThreads) k_coef_stats(const double *coef, long long n_steps, long long n_spin,
+                                                            double *stats) {
+  __shared__ double sh[kStatThreads];
+  const double *cd = coef, *cl = coef + n_steps, *cm = coef + 2 * n_steps;
+  const long long n = n_steps - n_spin;
+  if (n <= 0) {
+    if (threadIdx.x < 6) stats[threadIdx.x] = __longlong_as_double(0x7ff8000000000000ll);   // quiet NaN
+    return;
+  }
+  double s_cd = 0.0, s_cm = 0.0, s_cl = 0.0, m_cd = -1.0 / 0.0, m_cm = -1.0 / 0.0;
+  for (long long t = n_spin + threadIdx.x; t < n_steps; t += kStatThreads) {
+    s_cd += cd[t];
+    s_cm += cm[t];
+    s_cl += cl[t];
+    m_cd = fmax(m_cd, cd[t]);
+    m_cm = fmax(m_cm, cm[t]);
+  }
+  const double mean_cd = block_sum(s_cd, sh) / (double)n;
+  const double mean_cm = block_sum(s_cm, sh) / (double)n;
+  const double mean_cl = block_sum(s_cl, sh) / (double)n;
+  const double max_cd = block_max(m_cd, sh), max_cm = block_max(m_cm, sh);
+  double s_dev = 0.0;
+  for (long long t = n_spin + threadIdx.x; t < n_steps; t += kStatThreads) {
+    const double d = cd[t] - mean_cd;
+    s_dev += d * d;
+  }
+  const double var = block_sum(s_dev, sh) / (double)n;
+  if (threadIdx.x == 0) {
+    stats[0] = mean_cd;
+    stats[1] = max_cd;
+    stats[2] = sqrt(var);
+    stats[3] = mean_cm;
+    stats[4] = max_cm;
+    stats[5] = mean_cl;
+  }
+}
+
+cudaError_t aux_coefficients(const long long *force, long long n_steps, int nz, double qa, double H, double *coef,
+                             cudaStream_t s) {
+  if (n_steps <= 0) return cudaSuccess;
+  const long long threads = n_steps * 32;
+  k_coefficients<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(force, n_steps, nz, qa, H, coef);
+  return cudaGetLastError();
+}
+cudaError_t aux_coef_stats(const double *coef, long long n_steps, long long n_spin, double *stats, cudaStream_t s) {
+  k_coef_stats<<<1, kStatThreads, 0, s>>>(coef, n_steps, n_spin, stats);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- viewer payload
 // k_slice_xz / k_slice_xy (lbm3d.py:191-200): the macro field u (device layout
 // [4][nz][ny][pitch]) at y = y0 or z = z0, written in the reference layout

@@ -18,12 +18,17 @@ cudaError_t aux_unpack_u(const Geom &g, const float *u, float *ref, cudaStream_t
 cudaError_t aux_unpack_acc(const Geom &g, const double *acc, double *ref, cudaStream_t s);
 cudaError_t aux_build_tiles(const Geom &g, const uint8_t *flag, uint8_t *tiles, cudaStream_t s);
 cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cudaStream_t s);
+cudaError_t aux_coefficients(const long long *force, long long n_steps, int nz, double qa, double H, double *coef,
+                             cudaStream_t s);
+cudaError_t aux_coef_stats(const double *coef, long long n_steps, long long n_spin, double *stats, cudaStream_t s);
 cudaError_t aux_slice_xz(const Geom &g, const float *u, int y0, float *out, cudaStream_t s);
 cudaError_t aux_slice_xy(const Geom &g, const float *u, int z0, float *out, cudaStream_t s);
 cudaError_t aux_qcoarse(const Geom &g, const float *u, const uint8_t *flag, int x0, int ds, int di, int dj, int dk,
                         float *out, cudaStream_t s);
 
 int note_cuda_error(int cuda_error);  // sw_capi.cu
+// largest wall box (bytes of its bitset) the ellipsoid packer holds in shared memory
+constexpr long long kPackBoxBytesMax = 200 * 1024;
 unsigned int tma_timeouts_f16s();      // read and clear the TMA wait time-outs of sw_step_f16s.cu
 unsigned int tma_timeouts_bf16s();
 

@@ -362,6 +362,20 @@ int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s) {
   return cuda_status(sw::aux_force_to_f64(reinterpret_cast<const long long *>(force), out, n, st(s)));
 }
 
+int sw_coefficients(const int64_t *force, int64_t n_steps, int32_t nz, double UH, double H, int32_t ny, double *coef,
+                    sw_stream s) {
+  if (n_steps < 0 || nz <= 0 || ny <= 0 || !(UH > 0.0) || !(H > 0.0)) return SW_ERR_BAD_ARG;
+  if (n_steps > 0 && (!force || !coef || ((uintptr_t)force & 15u))) return SW_ERR_BAD_ARG;
+  const double qref = 0.5 * (UH * UH);
+  const double qa = qref * (H * (double)ny);
+  return cuda_status(sw::aux_coefficients(reinterpret_cast<const long long *>(force), n_steps, nz, qa, H, coef, st(s)));
+}
+
+int sw_coef_stats(const double *coef, int64_t n_steps, int64_t n_spin, double *stats, sw_stream s) {
+  if (n_steps < 0 || n_spin < 0 || !stats || (n_steps > 0 && !coef)) return SW_ERR_BAD_ARG;
+  return cuda_status(sw::aux_coef_stats(coef, n_steps, n_spin, stats, st(s)));
+}
+
 int sw_slice_xz(const sw_geom *g, const float *u, int32_t y0, float *out, sw_stream s) {
   if (!geom_ok(g) || !u || !out || y0 < 0 || y0 >= g->ny) return SW_ERR_BAD_ARG;
   return cuda_status(sw::aux_slice_xz(to_geom(g), u, y0, out, st(s)));

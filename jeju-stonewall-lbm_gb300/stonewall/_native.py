@@ -6,6 +6,7 @@ call raises NativeUnavailable.  Run ``python -m stonewall.build`` (or
 """
 import ctypes
 import os
+import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libstonewall.so")
@@ -23,6 +24,12 @@ DTYPE_NAMES = {"f32": SW_F32, "fp32": SW_F32, "float32": SW_F32,
                "f16": SW_F16_SHIFT, "fp16": SW_F16_SHIFT, "f16s": SW_F16_SHIFT,
                "bf16": SW_BF16_SHIFT, "bf16s": SW_BF16_SHIFT}
 DTYPE_BYTES = {SW_F32: 4, SW_F64: 8, SW_F16_SHIFT: 2, SW_BF16_SHIFT: 2}
+
+
+# Held while a CUDA graph is captured (the solver's chunks, the batch graphs) and by helper threads
+# around their own GPU work (the solve server's mask packing), so that no other thread's
+# allocations, copies or stream queries fall inside a capture and invalidate it.
+CAPTURE_LOCK = threading.RLock()
 
 
 class NativeUnavailable(RuntimeError):
@@ -101,6 +108,11 @@ def lib():
         "sw_accum": ([G, P, P, P], ctypes.c_int),
         "sw_macro_accum": ([G, ctypes.c_int, P, P, P, P, P], ctypes.c_int),
         "sw_force_to_f64": ([P, P, i64, P], ctypes.c_int),
+        "sw_coefficients": ([P, i64, i32, f64, f64, i32, P, P], ctypes.c_int),
+        "sw_coef_stats": ([P, i64, i64, P, P], ctypes.c_int),
+        "sw_pack_box_bytes": ([i32, i32, i32], i64),
+        "sw_pack_ellipsoids": ([P, i32, i32, i32, i32, i32, f64, P, P, P], ctypes.c_int),
+        "sw_voxelize_stones": ([P, i32, i32, i32, i32, P, P, i32, P], ctypes.c_int),
         "sw_tma_timeouts": ([], i64),
         "sw_slice_xz": ([G, P, i32, P, P], ctypes.c_int),
         "sw_slice_xy": ([G, P, i32, P, P], ctypes.c_int),

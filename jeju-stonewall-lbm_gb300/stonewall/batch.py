@@ -187,19 +187,21 @@ class Batch:
         key = (n, self.cfg)
         if key not in self._graphs:
             N.check(N.lib().sw_batch_setup(self.dtype, self.cfg), "sw_batch_setup")   # no device queries in capture
-            torch.cuda.synchronize()
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                for k in range(n):
-                    self._launch(k)
+            with N.CAPTURE_LOCK:
+                torch.cuda.synchronize()
+                with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                    for k in range(n):
+                        self._launch(k)
             self._graphs[key] = g
         return self._graphs[key]
 
     def _graph_run(self, slot, n_live, c):
         if n_live > GRAPH_MAX:
             raise RuntimeError(f"graph mode takes at most {GRAPH_MAX} lattices")
-        N.check(N.lib().sw_batch_graph_run(self._graph_handle(), ctypes.addressof(self._table_host[slot]), n_live,
-                                           self.dtype, int(c), _stream(None)), "sw_batch_graph_run")
+        with N.CAPTURE_LOCK:                     # the call captures the chunk's graph
+            N.check(N.lib().sw_batch_graph_run(self._graph_handle(), ctypes.addressof(self._table_host[slot]),
+                                               n_live, self.dtype, int(c), _stream(None)), "sw_batch_graph_run")
 
     # ------------------------------------------------------------ failures
     def status_words(self, members=None):

@@ -24,7 +24,7 @@ import torch
 
 from .batch import Batch
 from .geometry import ellipsoid_wall
-from .metrics import coefficients, stats
+from .metrics import device_stats
 from .params import baseline_params, flags_from_wall
 from .solver import WallSolver
 
@@ -51,8 +51,7 @@ def make_solver(spec, n_total, dtype, device="cuda", noise_seed=None):
 
 
 def wall_stats(s):
-    co = coefficients(s.force_series(), s.params.UH, s.params.H, s.params.ny)
-    return stats(co["Cd"], co["Cm"], co["Cl"], s.n_spin)
+    return device_stats(s.force, s.params.UH, s.params.H, s.params.ny, s.n_spin)
 
 
 def rel(a, b):

@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", CSRC, "-I", INCLUDE]
 # translation units that must evaluate float expressions in source order
-NO_FMAD = {"sw_aux.cu"}
+NO_FMAD = {"sw_aux.cu", "sw_geometry.cu"}
 
 
 def nvcc():

@@ -18,7 +18,17 @@ ellipsoid_wall(...) ellipsoids with semi-axes U[0.15H, 0.3H] and a uniformly
 
 Both return a bool mask (nx, ny, nz), y periodic, cell k centred at height
 k - 0.5 above the ground; the caller adds the ground plane (flag[:, :, 0]).
+
+With device="cuda" the per-cell work runs on the GPU (csrc/sw_geometry.cu):
+the ellipsoid packer's accept/reject loop over candidates drawn here in the
+same order, and the course wall's rasteriser; the masks are the host
+generators' bit for bit (the random draws and the bisection stay here, the
+packer's inside test is the same FMA-free float64 expression on both sides,
+and the few rasteriser cells too close to a stone surface for two pow
+implementations to agree are decided here).
 """
+import ctypes
+
 import numpy as np
 
 
@@ -81,23 +91,72 @@ def _lay(courses, gap, H, Ly):
     return stones
 
 
-def _voxelize(stones, nx, ny, nz, X0, T):
+def _stone_box(st, nz, X0, T):
+    """A stone's superellipsoid parameters and cell ranges (geometry.py:72-78)."""
+    a, b, c, p = st["ax"] * T / 2, st["b"], st["c"], st["p"]
+    xc = X0 + T / 2 + st["dx"] * T
+    xr = (int(np.floor(xc - a)), int(np.ceil(xc + a)) + 1)
+    kr = (max(1, int(np.floor(st["zc"] - c))), min(nz, int(np.ceil(st["zc"] + c)) + 2))
+    yr = (int(np.floor(st["yc"] - b)) - 1, int(np.ceil(st["yc"] + b)) + 2)
+    return xc, a, b, c, p, xr, yr, kr
+
+
+def _superellipsoid_r(X, Y, K, xc, yc, zc, a, b, c, p):
+    return (np.abs(X - xc) / a) ** p + (np.abs(Y - yc) / b) ** p + (np.abs(K - zc) / c) ** p
+
+
+def _voxelize(stones, nx, ny, nz, X0, T, device=None):
     """Cells whose centre lies inside a stone's superellipsoid (geometry.py:68-84)."""
+    if device is not None:
+        return _voxelize_device(stones, nx, ny, nz, X0, T, device)
     m = np.zeros((nx, ny, nz), bool)
-    xmid = X0 + T / 2
     for st in stones:
-        a, b, c, p = st["ax"] * T / 2, st["b"], st["c"], st["p"]
-        xc = xmid + st["dx"] * T
-        xi = np.arange(int(np.floor(xc - a)), int(np.ceil(xc + a)) + 1)
-        ki = np.arange(max(1, int(np.floor(st["zc"] - c))), min(nz, int(np.ceil(st["zc"] + c)) + 2))
-        yi = np.arange(int(np.floor(st["yc"] - b)) - 1, int(np.ceil(st["yc"] + b)) + 2)
+        xc, a, b, c, p, xr, yr, kr = _stone_box(st, nz, X0, T)
+        xi, yi, ki = np.arange(*xr), np.arange(*yr), np.arange(*kr)
         if len(xi) == 0 or len(ki) == 0:
             continue
         X, Y, K = np.meshgrid(xi + 0.5, yi + 0.5, ki - 0.5, indexing="ij")
-        r = (np.abs(X - xc) / a) ** p + (np.abs(Y - st["yc"]) / b) ** p + (np.abs(K - st["zc"]) / c) ** p
-        hit = r <= 1.0
+        hit = _superellipsoid_r(X, Y, K, xc, st["yc"], st["zc"], a, b, c, p) <= 1.0
         xs, ys, ks = np.meshgrid(xi, yi % ny, ki, indexing="ij")
         m[xs[hit], ys[hit], ks[hit]] = True
+    return m
+
+
+STONE_DTYPE = np.dtype([("xc", "f8"), ("yc", "f8"), ("zc", "f8"), ("a", "f8"), ("b", "f8"), ("c", "f8"),
+                        ("p", "f8"), ("x0", "i4"), ("x1", "i4"), ("y0", "i4"), ("y1", "i4"), ("k0", "i4"),
+                        ("k1", "i4")])                                  # sw_stone
+
+
+def _voxelize_device(stones, nx, ny, nz, X0, T, device, cap=4096):
+    """_voxelize on the GPU (sw_voxelize_stones); the cells it leaves undecided are decided here."""
+    import torch
+    from . import _native as N
+    from .fields import _ptr
+    recs = np.zeros(len(stones), STONE_DTYPE)
+    for i, st in enumerate(stones):
+        xc, a, b, c, p, xr, yr, kr = _stone_box(st, nz, X0, T)
+        if xr[1] > xr[0] and kr[1] > kr[0] and (xr[0] < 0 or xr[1] > nx):
+            raise ValueError(f"stone {i} reaches past the x extent of the grid")
+        recs[i] = (xc, st["yc"], st["zc"], a, b, c, p, xr[0], xr[1], yr[0], yr[1], kr[0], kr[1])
+    dev = torch.device(device)
+    stream = torch.cuda.Stream(device=dev)                  # beside the solves' stream
+    with N.CAPTURE_LOCK, torch.cuda.stream(stream):
+        st_dev = torch.from_numpy(recs.view(np.uint8).copy()).to(dev)
+        mask = torch.zeros(nx * ny * nz, dtype=torch.uint8, device=dev)
+        amb = torch.zeros(1 + 4 * cap, dtype=torch.int32, device=dev)
+        N.check(N.lib().sw_voxelize_stones(_ptr(st_dev), len(recs), nx, ny, nz, _ptr(mask), _ptr(amb), cap,
+                                           ctypes.c_void_p(stream.cuda_stream)), "sw_voxelize_stones")
+        m = mask.cpu().numpy().astype(bool).reshape(nx, ny, nz)
+        amb_h = amb.cpu().numpy()
+    n_amb = int(amb_h[0])
+    if n_amb > cap:
+        raise RuntimeError(f"{n_amb} cells next to stone surfaces exceed the list of {cap}")
+    for s_i, x, yy, k in amb_h[1:1 + 4 * n_amb].reshape(-1, 4):
+        r = recs[s_i]
+        v = _superellipsoid_r(np.array([x + 0.5]), np.array([yy + 0.5]), np.array([k - 0.5]), r["xc"], r["yc"],
+                              r["zc"], r["a"], r["b"], r["c"], r["p"])
+        if v[0] <= 1.0:
+            m[x, yy % ny, k] = True
     return m
 
 
@@ -149,12 +208,13 @@ def _shrunk(stones, s):
     return out
 
 
-def course_wall(porosity, H, nx, ny, nz, X0, T, seed=7, verbose=False):
-    """The reference's wall (geometry.py:135-161).  Returns (mask, frontal porosity)."""
+def course_wall(porosity, H, nx, ny, nz, X0, T, seed=7, verbose=False, device=None):
+    """The reference's wall (geometry.py:135-161).  Returns (mask, frontal porosity).  device: rasterise
+    the stones on that GPU (the same mask)."""
     rng = np.random.default_rng(seed)
     base = _tag_anchors(_lay(_draw_courses(H, ny, rng), 0.0, H, ny), ny)
     if porosity <= 0.0:
-        m = _voxelize(base, nx, ny, nz, X0, T)
+        m = _voxelize(base, nx, ny, nz, X0, T, device)
         xa, xb = X0 + int(round(0.15 * T)), X0 + int(round(0.85 * T))
         col = m.any(axis=0)
         for j in range(ny):
@@ -168,7 +228,7 @@ def course_wall(porosity, H, nx, ny, nz, X0, T, seed=7, verbose=False):
             s = 0.5 * (lo + hi)
             phi = frontal_porosity(_silhouette(_shrunk(base, s), ny, nz), H)
             lo, hi = (s, hi) if phi > porosity else (lo, s)
-        m = _voxelize(_shrunk(base, s), nx, ny, nz, X0, T)
+        m = _voxelize(_shrunk(base, s), nx, ny, nz, X0, T, device)
     phi = frontal_porosity(m.any(axis=0), H)
     if verbose:
         print(f"[wall] stones={len(base)} scale={s:.3f} frontal porosity={phi:.3f}", flush=True)
@@ -186,11 +246,42 @@ def _random_rotation(rng):
                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
 
 
-def ellipsoid_wall(porosity, H, nx, ny, nz, X0, T, seed=0, height=None, max_tries=200000, verbose=False):
+def _draw_candidate(rng, H, ny, X0, T, z_hi):
+    """One candidate stone of the packer, in the generator's draw order: centre, semi-axes,
+    rotation, and the cell ranges of its bounding cube clipped to the wall box."""
+    centre = np.array([rng.uniform(X0, X0 + T), rng.uniform(0, ny), rng.uniform(0.5, z_hi - 0.5)])
+    semi = rng.uniform(0.15 * H, 0.3 * H, size=3)
+    R = _random_rotation(rng)
+    ext = semi.max()
+    lo = np.floor(centre - ext).astype(int)
+    hi = np.ceil(centre + ext).astype(int) + 1
+    xr = (max(lo[0], X0), min(hi[0], X0 + T))
+    kr = (max(lo[2], 1), min(hi[2], z_hi))
+    return centre, semi, R, xr, (int(lo[1]), int(hi[1])), kr
+
+
+def _ellipsoid_inside(X, Y, K, centre, semi, R):
+    """Cell centres inside the rotated ellipsoid: body-frame coordinates d_j = sum_i a_i R[i, j] and
+    sum_j (d_j / semi_j)^2 <= 1, each sum taken left to right (no matrix product, so the same float64
+    operations run on any machine and in the GPU packer)."""
+    dx, dy, dz = X - centre[0], Y - centre[1], K - centre[2]
+    t0 = ((dx * R[0, 0] + dy * R[1, 0]) + dz * R[2, 0]) / semi[0]
+    t1 = ((dx * R[0, 1] + dy * R[1, 1]) + dz * R[2, 1]) / semi[1]
+    t2 = ((dx * R[0, 2] + dy * R[1, 2]) + dz * R[2, 2]) / semi[2]
+    return ((t0 * t0 + t1 * t1) + t2 * t2) <= 1.0
+
+
+ELLIPSOID_DTYPE = np.dtype([("centre", "f8", 3), ("semi", "f8", 3), ("rot", "f8", 9), ("x0", "i4"), ("x1", "i4"),
+                            ("y0", "i4"), ("y1", "i4"), ("k0", "i4"), ("k1", "i4")])     # sw_ellipsoid
+
+
+def ellipsoid_wall(porosity, H, nx, ny, nz, X0, T, seed=0, height=None, max_tries=200000, verbose=False,
+                   device=None):
     """Rejection-packed ellipsoid stones in the box x in [X0, X0+T), all y (periodic), z in [1, height].
 
     Returns (mask, solid fraction of the box).  The fill stops once the box's
-    solid fraction reaches 1 - porosity (to within half a stone).
+    solid fraction reaches 1 - porosity (to within half a stone).  device: run the
+    accept/reject loop on that GPU (the same mask).
     """
     height = int(round(H)) if height is None else int(height)
     z_hi = min(nz, 1 + height)
@@ -202,34 +293,69 @@ def ellipsoid_wall(porosity, H, nx, ny, nz, X0, T, seed=0, height=None, max_trie
         m[box] = True
         return m, 1.0
     rng = np.random.default_rng(seed)
-    solid = 0
-    tries = 0
-    while solid < target - 0.5 and tries < max_tries:
-        tries += 1
-        centre = np.array([rng.uniform(X0, X0 + T), rng.uniform(0, ny), rng.uniform(0.5, z_hi - 0.5)])
-        semi = rng.uniform(0.15 * H, 0.3 * H, size=3)
-        R = _random_rotation(rng)
-        ext = semi.max()
-        lo = np.floor(centre - ext).astype(int)
-        hi = np.ceil(centre + ext).astype(int) + 1
-        xi = np.arange(max(lo[0], X0), min(hi[0], X0 + T))
-        ki = np.arange(max(lo[2], 1), min(hi[2], z_hi))
-        yi = np.arange(lo[1], hi[1])
-        if len(xi) == 0 or len(ki) == 0:
-            continue
-        X, Y, K = np.meshgrid(xi + 0.5, yi + 0.5, ki - 0.5, indexing="ij")
-        d = np.stack([X - centre[0], Y - centre[1], K - centre[2]], -1) @ R   # body frame
-        inside = ((d / semi) ** 2).sum(-1) <= 1.0
-        xs, ys, ks = np.meshgrid(xi, yi % ny, ki, indexing="ij")
-        xs, ys, ks = xs[inside], ys[inside], ks[inside]
-        new = ~m[xs, ys, ks]
-        n_new = int(np.unique(np.stack([xs[new], ys[new], ks[new]]), axis=1).shape[1]) if new.any() else 0
-        if n_new == 0 or solid + n_new > target + 0.5 * n_new:
-            continue
-        m[xs, ys, ks] = True
-        solid += n_new
+    if device is not None:
+        tries = _pack_device(m, rng, H, ny, X0, T, z_hi, target, max_tries, device)
+    else:
+        solid = 0
+        tries = 0
+        while solid < target - 0.5 and tries < max_tries:
+            tries += 1
+            centre, semi, R, xr, yr, kr = _draw_candidate(rng, H, ny, X0, T, z_hi)
+            xi, yi, ki = np.arange(*xr), np.arange(*yr), np.arange(*kr)
+            if len(xi) == 0 or len(ki) == 0:
+                continue
+            X, Y, K = np.meshgrid(xi + 0.5, yi + 0.5, ki - 0.5, indexing="ij")
+            inside = _ellipsoid_inside(X, Y, K, centre, semi, R)
+            xs, ys, ks = np.meshgrid(xi, yi % ny, ki, indexing="ij")
+            xs, ys, ks = xs[inside], ys[inside], ks[inside]
+            new = ~m[xs, ys, ks]
+            n_new = int(np.unique(np.stack([xs[new], ys[new], ks[new]]), axis=1).shape[1]) if new.any() else 0
+            if n_new == 0 or solid + n_new > target + 0.5 * n_new:
+                continue
+            m[xs, ys, ks] = True
+            solid += n_new
     frac = float(m[box].sum()) / box_cells
     if verbose:
         print(f"[wall] ellipsoids: solid fraction {frac:.3f} (target {1 - porosity:.3f}) after {tries} tries",
               flush=True)
     return m, frac
+
+
+def _pack_device(m, rng, H, ny, X0, T, z_hi, target, max_tries, device, first_batch=256, batch=1024):
+    """The packer's loop on the GPU (sw_pack_ellipsoids), candidates drawn here in batches; fills m's
+    wall box and returns the number of tries, as the host loop would."""
+    import torch
+    from . import _native as N
+    from .fields import _ptr
+    dev = torch.device(device)
+    nbytes = int(N.lib().sw_pack_box_bytes(T, ny, z_hi))
+    if nbytes < 0:
+        raise ValueError("bad wall box")
+    stream = torch.cuda.Stream(device=dev)                  # beside the solves' stream
+    with N.CAPTURE_LOCK, torch.cuda.stream(stream):
+        bits = torch.zeros(nbytes // 4, dtype=torch.int32, device=dev)
+        state = torch.zeros(2, dtype=torch.int64, device=dev)
+    tries = 0
+    solid = 0
+    n = min(first_batch, max_tries)
+    while solid < target - 0.5 and tries < max_tries:
+        n = min(n, max_tries - tries)
+        recs = np.zeros(n, ELLIPSOID_DTYPE)                  # drawn on the host, outside the lock
+        for i in range(n):
+            centre, semi, R, xr, yr, kr = _draw_candidate(rng, H, ny, X0, T, z_hi)
+            if yr[1] - yr[0] > ny:
+                raise ValueError("a stone wider than the span: its cells would wrap onto themselves")
+            recs[i] = (centre, semi, R.ravel(), xr[0], xr[1], yr[0], yr[1], kr[0], kr[1])
+        with N.CAPTURE_LOCK, torch.cuda.stream(stream):
+            cand = torch.from_numpy(recs.view(np.uint8).copy()).to(dev)
+            N.check(N.lib().sw_pack_ellipsoids(_ptr(cand), n, X0, T, ny, z_hi, float(target), _ptr(bits),
+                                               _ptr(state), ctypes.c_void_p(stream.cuda_stream)),
+                    "sw_pack_ellipsoids")
+            solid, used = (int(v) for v in state.cpu().tolist())
+        tries += used
+        n = batch
+    with N.CAPTURE_LOCK, torch.cuda.stream(stream):
+        words = bits.cpu().numpy().view(np.uint32)
+    flat = np.unpackbits(words.view(np.uint8), bitorder="little")[:T * ny * (z_hi - 1)].astype(bool)
+    m[X0:X0 + T, :, 1:z_hi] = flat.reshape(T, ny, z_hi - 1)
+    return tries

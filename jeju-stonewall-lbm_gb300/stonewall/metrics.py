@@ -6,6 +6,9 @@ coefficients():  lbm3d.py:396-407 -- Fx, Fz and the overturning moment about
 stats():         postprocess.py:65-82 -- mean / peak / std of Cd (std is the
                  force RMS about the mean), mean / peak Cm, mean Cl over
                  t >= n_spin.  Computed in float64.
+device_stats():  the same two steps on the GPU from the device force series
+                 (sw_coefficients, sw_coef_stats): 48 bytes come back instead
+                 of the whole series.
 recirculation_area(): export3d.py:169-184 -- cells of the every-2nd-cell mean
                  field with u_x < 0 in [X0, X0 + 10H) x [0, 2H) after the
                  same masking and one 3-point box blur, times 8 / (H^2 ny).
@@ -33,6 +36,33 @@ def stats(Cd, Cm, Cl, n_spin):
                     CmMax=float("nan"), Cl=float("nan"))
     return dict(Cd=float(Cd.mean()), CdMax=float(Cd.max()), CdStd=float(Cd.std()),
                 Cm=float(Cm.mean()), CmMax=float(Cm.max()), Cl=float(Cl.mean()))
+
+
+STAT_KEYS = ("Cd", "CdMax", "CdStd", "Cm", "CmMax", "Cl")
+
+
+def device_coefficients(force, UH, H, ny, stream=None):
+    """coefficients() on the GPU from a stonewall.fields.ForceSeries: a float64 CUDA tensor (3, n) of
+    Cd, Cl, Cm."""
+    import torch
+    from . import _native as N
+    from .fields import _ptr, _stream
+    coef = torch.empty((3, force.n_steps), dtype=torch.float64, device=force.data.device)
+    N.check(N.lib().sw_coefficients(force.ptr, force.n_steps, force.nz, float(UH), float(H), int(ny), _ptr(coef),
+                                    _stream(stream)), "sw_coefficients")
+    return coef
+
+
+def device_stats(force, UH, H, ny, n_spin, stream=None):
+    """stats(coefficients(...)) computed on the GPU; the same dict, 6 floats downloaded."""
+    import torch
+    from . import _native as N
+    from .fields import _ptr, _stream
+    coef = device_coefficients(force, UH, H, ny, stream)
+    out = torch.empty(6, dtype=torch.float64, device=coef.device)
+    N.check(N.lib().sw_coef_stats(_ptr(coef), force.n_steps, int(n_spin), _ptr(out), _stream(stream)),
+            "sw_coef_stats")
+    return dict(zip(STAT_KEYS, (float(v) for v in out.cpu().tolist())))
 
 
 def fx_profile(force, UH, ny, n_spin):

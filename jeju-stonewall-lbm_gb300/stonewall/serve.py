@@ -43,7 +43,7 @@ import torch
 
 from .batch import Batch
 from .geometry import ellipsoid_wall
-from .metrics import coefficients, stats
+from .metrics import coefficients, device_stats, stats
 from .params import baseline_params, flags_from_wall
 from .solver import DeviceWaitTimeout, Diverged, WallSolver
 
@@ -93,10 +93,11 @@ def cells_of(req):
     return p.nx * p.ny * p.nz
 
 
-def prepare(req):
-    """Host side of a request: parameters and the flag array (run on a worker thread)."""
+def prepare(req, mask_device=None):
+    """A request's parameters and flag array (run on a worker thread).  mask_device: pack the stones
+    on that GPU (the host packer's mask, on a stream of its own beside the solves)."""
     p = baseline_params(req.H, req.steps, UH=req.U)
-    wall, frac = ellipsoid_wall(req.porosity, p.H, p.nx, p.ny, p.nz, p.X0, p.T, seed=req.seed)
+    wall, frac = ellipsoid_wall(req.porosity, p.H, p.nx, p.ny, p.nz, p.X0, p.T, seed=req.seed, device=mask_device)
     return p, flags_from_wall(wall, p.nx, p.ny, p.nz)
 
 
@@ -115,6 +116,13 @@ def failure_result(req, s, err, now):
 
 
 def solve_stats(s):
+    """The solve's Cd / Cm statistics, reduced on the GPU (48 bytes read back instead of the force series)."""
+    p = s.params
+    return device_stats(s.force, p.UH, p.H, p.ny, s.n_spin)
+
+
+def solve_stats_host(s):
+    """The same statistics from the downloaded force series (stonewall.metrics on the host)."""
     p = s.params
     co = coefficients(s.force_series(), p.UH, p.H, p.ny)
     return stats(co["Cd"], co["Cm"], co["Cl"], s.n_spin)
@@ -122,7 +130,7 @@ def solve_stats(s):
 
 class Server:
     def __init__(self, cap_bytes=160e9, chunk=50, max_members=256, device="cuda", workers=4, clock=time.monotonic,
-                 mode="graph", max_cells=None, check_every=20):
+                 mode="graph", max_cells=None, check_every=20, mask_device="cuda"):
         self.cap = float(cap_bytes)
         self.max_cells = float(max_cells) if max_cells else float("inf")
         self.cells = 0
@@ -140,10 +148,16 @@ class Server:
         self.pool = cf.ThreadPoolExecutor(max_workers=workers)
         self.clock = clock
         self.check_every = int(check_every)       # loop iterations between status checks of all residents
+        self.mask_device = mask_device             # where the stone masks are packed (None: host)
         self.failed = 0
         self.resident = {}                         # rid -> (request, solver, bytes)
         self.used = 0.0
         self.log = []
+
+    def _prepare(self, req):
+        out = prepare(req, self.mask_device)
+        req.t_prepared = self.clock() - self._t0              # arrival -> mask ready: the preparation lag
+        return out
 
     def _admit(self, queue, prepared, now):
         while queue:
@@ -200,7 +214,7 @@ class Server:
         done = [rid for rid, (req, s, need) in self.resident.items() if s.t >= s.n_total]
         for rid in done:
             req, s, need = self.resident[rid]
-            st = solve_stats(s)                    # reads the force series: waits for the solve's last chunk
+            st = solve_stats(s)                    # reduced on the GPU: waits for the solve's last chunk
             err = s.status_error()
             if err is not None:
                 self._fail(rid, err)
@@ -208,7 +222,8 @@ class Server:
             req, s = self._release(rid)
             now = self.clock() - self._t0
             req.result = dict(stats=st, t_done=now, latency=now - req.t_arrive, wait=req.t_admit - req.t_arrive,
-                              run=now - req.t_admit, cells=s.grid.cells)
+                              run=now - req.t_admit, cells=s.grid.cells,
+                              prep=getattr(req, "t_prepared", req.t_admit) - req.t_arrive)
             del s
         return len(done)
 
@@ -226,7 +241,7 @@ class Server:
             now = self.clock() - t0
             while i < len(reqs) and reqs[i].t_arrive <= now:
                 queue.append(reqs[i])
-                prepared[reqs[i].rid] = self.pool.submit(prepare, reqs[i])
+                prepared[reqs[i].rid] = self.pool.submit(self._prepare, reqs[i])
                 i += 1
             self._admit(queue, prepared, now)
             active = [b for b in self.batches.values() if b.pending()]
@@ -263,12 +278,15 @@ class Server:
         done = [r for r in reqs if r.result is not None and "failed" not in r.result]
         lat = np.array([r.result["latency"] for r in done]) if done else np.zeros(1)
         wait = np.array([r.result["wait"] for r in done]) if done else np.zeros(1)
+        prep = np.array([r.result.get("prep", 0.0) for r in done]) if done else np.zeros(1)
         cell_steps = sum(r.result["cells"] * r.steps for r in done)
         return dict(requests=len(reqs), completed=len(done), elapsed_s=round(elapsed, 1),
                     solves_per_hour=round(len(done) / elapsed * 3600, 1) if elapsed > 0 else 0.0,
                     p50_latency_s=round(float(np.percentile(lat, 50)), 2),
                     p99_latency_s=round(float(np.percentile(lat, 99)), 2),
                     p50_wait_s=round(float(np.percentile(wait, 50)), 2),
+                    p50_prep_s=round(float(np.percentile(prep, 50)), 3),
+                    p99_prep_s=round(float(np.percentile(prep, 99)), 3),
                     mean_glups=round(cell_steps / elapsed / 1e9, 2) if elapsed > 0 else 0.0,
                     f16_share=round(np.mean([r.dtype == "f16" for r in done]), 3) if done else 0.0,
                     failed=len(failed))
@@ -277,8 +295,9 @@ class Server:
 class PlainServer:
     """The plain form: one request at a time, first come first served, float32, no batching."""
 
-    def __init__(self, chunk=50, device="cuda", workers=4, clock=time.monotonic):
+    def __init__(self, chunk=50, device="cuda", workers=4, clock=time.monotonic, mask_device="cuda"):
         self.chunk, self.device, self.clock = int(chunk), torch.device(device), clock
+        self.mask_device = mask_device
         self.pool = cf.ThreadPoolExecutor(max_workers=workers)
         self.log, self.max_used = [], 0.0
 
@@ -291,7 +310,7 @@ class PlainServer:
             now = self.clock() - t0
             while i < len(reqs) and reqs[i].t_arrive <= now:
                 queue.append(reqs[i])
-                prepared[reqs[i].rid] = self.pool.submit(prepare, reqs[i])
+                prepared[reqs[i].rid] = self.pool.submit(prepare, reqs[i], self.mask_device)
                 i += 1
             if max_seconds is not None and now > max_seconds and not drain:
                 break
@@ -356,13 +375,15 @@ def main(argv=None):
     ap.add_argument("--plain", action="store_true", help="serve the plain way (one float32 solve at a time)")
     ap.add_argument("--no-drain", action="store_true", help="stop at the end of the window (unfinished solves count as not done)")
     ap.add_argument("--fp64-check", type=int, default=0, help="re-run this many completed requests in float64")
+    ap.add_argument("--host-masks", action="store_true", help="pack the stone masks on the host instead of the GPU")
     a = ap.parse_args(argv)
     reqs = poisson_requests(a.rate, a.minutes * 60.0, seed=a.seed, H_range=(a.h_lo, a.h_hi),
                             steps=(a.steps_lo, a.steps_hi), f16_share=a.f16_share)
     if a.plain:
-        srv = PlainServer(chunk=a.chunk)
+        srv = PlainServer(chunk=a.chunk, mask_device=None if a.host_masks else "cuda")
     else:
-        srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk, mode=a.mode, max_cells=a.max_cells or None)
+        srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk, mode=a.mode, max_cells=a.max_cells or None,
+                     mask_device=None if a.host_masks else "cuda")
     t0 = time.monotonic()
     out = srv.serve(reqs, max_seconds=a.minutes * 60.0, drain=not a.no_drain)
     elapsed = time.monotonic() - t0

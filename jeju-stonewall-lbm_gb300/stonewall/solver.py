@@ -186,12 +186,12 @@ class WallSolver:
         saved = (self.cur, self.aa_odd_next)
         self.cur = cur0
         graph = torch.cuda.CUDAGraph()
-        # warm the capture path once on a side stream as torch recommends
-        torch.cuda.synchronize()
-        with torch.cuda.graph(graph):
-            ring.data.zero_()
-            for j in range(n):
-                self._step(ring, j, accumulate=phase is not None and (phase + j) % self.acc_every == 0)
+        with N.CAPTURE_LOCK:                     # no other thread's GPU work inside the capture
+            torch.cuda.synchronize()
+            with torch.cuda.graph(graph, capture_error_mode="thread_local"):
+                ring.data.zero_()
+                for j in range(n):
+                    self._step(ring, j, accumulate=phase is not None and (phase + j) % self.acc_every == 0)
         self.cur, self.aa_odd_next = saved
         n_acc = 0 if phase is None else sum(1 for j in range(n) if (phase + j) % self.acc_every == 0)
         self._graphs[key] = (graph, n_acc)

@@ -73,6 +73,12 @@ def test_entry_points_reject_bad_arguments_before_launching(native_lib):
     assert L.sw_step_checked(gp, 0, p, q, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None, -1,
                              ctypes.c_void_p(buf.ctypes.data + 2), None) == N.SW_ERR_BAD_ARG     # status misaligned
     assert L.sw_step_cfg(gp, 0, p, q, p, p, p, 0.0, 0.0, 0, 0.0, None, 0, None, -1, None) == N.SW_ERR_BAD_ARG
+    assert L.sw_coefficients(p, 4, 0, 0.05, 40.0, 160, p, None) == N.SW_ERR_BAD_ARG               # nz
+    assert L.sw_coefficients(p, 4, 8, 0.0, 40.0, 160, p, None) == N.SW_ERR_BAD_ARG                # U_H
+    assert L.sw_coefficients(ctypes.c_void_p(buf.ctypes.data + 8), 4, 8, 0.05, 40.0, 160, p,
+                             None) == N.SW_ERR_BAD_ARG                                             # misaligned rows
+    assert L.sw_coef_stats(p, 4, -1, p, None) == N.SW_ERR_BAD_ARG
+    assert L.sw_coef_stats(p, 4, 0, None, None) == N.SW_ERR_BAD_ARG
 
 
 def test_status_words_map_to_errors(native_lib):
