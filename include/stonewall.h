@@ -55,7 +55,9 @@ enum {
  * (lbm3d.py:386-391); here every fluid cell of every step is covered. */
 enum {
   SW_STATUS_NONFINITE = 1, /* some fluid cell had a non-finite density after pulling its populations */
-  SW_STATUS_TIMEOUT = 2    /* a block of the TMA-staged step gave up waiting for its copies: cells unwritten */
+  SW_STATUS_TIMEOUT = 2,   /* a block of the TMA-staged step gave up waiting for its copies: cells unwritten */
+  SW_STATUS_BOUNDS = 4     /* bounds-checked build only (libstonewall_check.so): a computed element offset
+                              fell outside its population plane; the access went to element 0 instead */
 };
 
 /* storage type of the distributions */

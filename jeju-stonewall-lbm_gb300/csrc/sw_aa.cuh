@@ -73,7 +73,7 @@ __device__ __forceinline__ void aa_odd_cell(const StepParams &p, const AAParams 
   using T = typename S::T;
   using R = typename S::R;
   const Geom &g = p.g;
-  const int c = (z * g.ny + y) * g.pitch + x;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x);
   if (CHECK && p.flag[c] != 0) return;
   const int row = g.pitch, lev = g.ny * g.pitch;
   const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;        // row of y - 1 (periodic)
@@ -92,8 +92,8 @@ __device__ __forceinline__ void aa_odd_cell(const StepParams &p, const AAParams 
     static_for<0, Q>([&](auto I) {
       constexpr int i = decltype(I)::value;
       constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
-      const int src = c + (ex == 1 ? -1 : ex == -1 ? off_xp : 0) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
-                      (ez == 1 ? -lev : ez == -1 ? off_zp : 0);
+      const int src = chk(p, c + (ex == 1 ? -1 : ex == -1 ? off_xp : 0) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
+                                 (ez == 1 ? -lev : ez == -1 ? off_zp : 0));
       bool pull = true;
       if constexpr (CHECK) {
         const uint8_t fs = (ez == 1 && z == 0) ? (uint8_t)SW_GROUND : __ldg(p.flag + src);
@@ -136,7 +136,7 @@ __device__ __forceinline__ void aa_odd_cell(const StepParams &p, const AAParams 
   // scatter of S_k to the slots the next even step reads (physical planes: fout_pop).
   // A segment without the checked path has only fluid neighbours around its
   // pulling cells; an inlet cell does not pull, so its targets are checked.
-  const bool chk = CHECK || x == 0;
+  const bool chk_t = CHECK || x == 0;
   auto scatter = [&](auto I, R v) {
     constexpr int k = decltype(I)::value;
     constexpr int ex = CX(k), ey = CY(k), ez = CZ(k);
@@ -146,25 +146,25 @@ __device__ __forceinline__ void aa_odd_cell(const StepParams &p, const AAParams 
       S::template st<k>(p.template out<T>(OPP(k)) + c, v);
     const int tx = x + ex, tz = z + ez;
     if (tx >= 0 && tx < g.nx && tz >= 0 && tz < g.nz) {          // (a)
-      const int t = c + ex + oy + ez * lev;
-      if (!chk || p.flag[t] == 0) S::template st<k>(pl + t, v);
+      const int t = chk(p, c + ex + oy + ez * lev);
+      if (!chk_t || p.flag[t] == 0) S::template st<k>(pl + t, v);
     }
     if constexpr (ex == -1) {
       if (outlet && tz >= 0 && tz < g.nz) {                       // (b)
-        const int t = c + oy + ez * lev;
-        if (!chk || p.flag[t] == 0) S::template st<k>(pl + t, v);
+        const int t = chk(p, c + oy + ez * lev);
+        if (!chk_t || p.flag[t] == 0) S::template st<k>(pl + t, v);
       }
     }
     if constexpr (ez == 1) {
       if (top) {                                                  // (c)
         T *pm = p.template out<T>(MIRZ(k));
         if (tx >= 0 && tx < g.nx) {
-          const int t = c + ex + oy;
-          if (!chk || p.flag[t] == 0) S::template st<MIRZ(k)>(pm + t, v);
+          const int t = chk(p, c + ex + oy);
+          if (!chk_t || p.flag[t] == 0) S::template st<MIRZ(k)>(pm + t, v);
         }
         if (ex == -1 && outlet) {
-          const int t = c + oy;
-          if (!chk || p.flag[t] == 0) S::template st<MIRZ(k)>(pm + t, v);
+          const int t = chk(p, c + oy);
+          if (!chk_t || p.flag[t] == 0) S::template st<MIRZ(k)>(pm + t, v);
         }
       }
     }
@@ -202,7 +202,7 @@ __device__ __forceinline__ void aa_even_cell(const StepParams &p, int x, int y, 
   using T = typename S::T;
   using R = typename S::R;
   const Geom &g = p.g;
-  const int c = (z * g.ny + y) * g.pitch + x;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x);
   if (CHECK && p.flag[c] != 0) return;
   R rho, ux, uy, uz;
   // own cell: incoming values in natural slots (fin_pop), results to opposite slots (fout_pop is permuted)
@@ -239,8 +239,8 @@ __device__ __forceinline__ void aa_even_cell(const StepParams &p, int x, int y, 
         constexpr int i = decltype(I)::value;
         constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
         if constexpr (ex != 0 || ez != 0) {
-          const int src = c + (ex == 1 ? -1 : ex == -1 ? off_xp : 0) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
-                          (ez == 1 ? -lev : ez == -1 ? off_zp : 0);
+          const int src = chk(p, c + (ex == 1 ? -1 : ex == -1 ? off_xp : 0) +
+                                     (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) + (ez == 1 ? -lev : ez == -1 ? off_zp : 0));
           const uint8_t fs = (ez == 1 && z == 0) ? (uint8_t)SW_GROUND : __ldg(p.flag + src);
           if (fs == SW_WALL) {                                  // fl[i] holds the bounced f_opp(i)(x)
             const R fr = S::kShift ? fl[i] : fl[i] - W<R>(i);
@@ -290,6 +290,157 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB) k_step_aa(const __gri
   if ((kind & TILE_FORCE) && p.force != nullptr) warp_force_add<R>(p, z, lane, fxw, fzw, hit);
 }
 
+// ---------------------------------------------------------------- two cells per thread (16-bit storage)
+// The same plan with one 32-bit word carrying both cells of a pair, as the
+// two-lattice pair kernel does; a warp covers two 32-cell segments of a row.
+// Loads are coherent (plain) loads: the lattice is written in place.
+template <int DT>
+__device__ __forceinline__ uint32_t aa_word(const typename Store<DT>::T *q) {
+  return *reinterpret_cast<const uint32_t *>(q);
+}
+
+// Even step, fast path: both cells read their 19 incoming values from their own
+// slots (plane opp(i), fin_pop) and write S_k to plane k (fout_pop), packed.
+template <int DT, bool ACC>
+__device__ __forceinline__ void aa_pair_even_fast(const StepParams &p, int x0, int y, int z) {
+  using T = typename Store<DT>::T;
+  using PK = Pack16<DT>;
+  const Geom &g = p.g;
+  if (x0 >= g.nx) return;
+  const bool has_b = x0 + 1 < g.nx;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
+  f2 v[Q];
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    v[i].v = PK::both(aa_word<DT>(p.template in<T>(i) + c));
+  });
+  double2 acc_old[4];
+  if (ACC) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      acc_old[k] = has_b ? *reinterpret_cast<const double2 *>(p.accp(k) + c) : make_double2(p.accp(k)[c], 0.0);
+  }
+  pair_collide_store<DT, ACC>(p, v, x0, c, z, x0 == 0, has_b, [&](int k) { return acc_old[k]; });
+}
+
+// Odd step, fast path of an interior segment pair (not the inlet or the outlet
+// segment pair, not the top level; every pull source and scatter target is a
+// fluid cell inside the lattice): pull as the two-lattice pair kernel does, then
+// scatter S_k of both cells to slot k of x + c_k (fout_pop[k] = plane opp(k)).
+// For c_x = +-1 the two targets straddle two aligned words: lane L writes the
+// word that holds its second target and lane L + 1's first (one shuffle); the
+// halves at the warp's edges, shared with the neighbouring warps, are 16-bit stores.
+template <int DT, bool ACC>
+__device__ __forceinline__ void aa_pair_odd_interior(const StepParams &p, int x0, int y, int z, int lane) {
+  using S = Store<DT>;
+  using T = typename S::T;
+  using PK = Pack16<DT>;
+  const Geom &g = p.g;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
+  const int row = g.pitch, lev = g.ny * g.pitch;
+  const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;        // row of y - 1 (periodic)
+  const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row; // row of y + 1 (periodic)
+  uint32_t P[Q];
+  float edge[Q];
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
+    const T *plane = p.template in<T>(i);
+    const int src = c + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) - ez * lev;
+    P[i] = aa_word<DT>(plane + chk(p, src));
+    if constexpr (ex == 1) edge[i] = lane == 0 ? S::to_shifted(plane[chk(p, src - 1)]) : 0.0f;
+    if constexpr (ex == -1) edge[i] = lane == 31 ? S::to_shifted(plane[chk(p, src + 2)]) : 0.0f;
+  });
+  double2 acc_old[4];
+  if (ACC) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc_old[k] = *reinterpret_cast<const double2 *>(p.accp(k) + c);
+  }
+  f2 v[Q];
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = CX(i);
+    const float2 own = PK::both(P[i]);
+    if constexpr (ex == 0) {
+      v[i].v = own;
+    } else if constexpr (ex == 1) {                                 // sources x0 - 1, x0
+      const uint32_t prev = __shfl_up_sync(0xffffffffu, P[i], 1);
+      v[i] = F2(lane == 0 ? edge[i] : PK::hi(prev), own.x);
+    } else {                                                        // sources x0 + 1, x0 + 2
+      const uint32_t next = __shfl_down_sync(0xffffffffu, P[i], 1);
+      v[i] = F2(own.y, lane == 31 ? edge[i] : PK::lo(next));
+    }
+  });
+  const Phys<float> ph = phys<float>(p);
+  f2 rho, ux, uy, uz;
+  collide2(v, x0, true, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz, p.status,
+           [&](auto I, f2 o) {
+             constexpr int k = decltype(I)::value;
+             constexpr int ex = CX(k), ey = CY(k), ez = CZ(k);
+             T *plane = p.template out<T>(k);
+             const int t = c + (ey == 1 ? off_yp : ey == -1 ? off_ym : 0) + ez * lev;   // target row, column x0
+             if constexpr (ex == 0) {
+               *reinterpret_cast<uint32_t *>(plane + chk(p, t)) = PK::pack(o.v.x, o.v.y);
+             } else {
+               // targets x0 + ex (first cell) and x0 + 1 + ex (second cell); lane L writes the
+               // word holding its second target and lane L + 1's first
+               const float nxt = __shfl_down_sync(0xffffffffu, o.v.x, 1);
+               const int w = chk(p, t + (ex == 1 ? 2 : 0));
+               if (lane < 31) *reinterpret_cast<uint32_t *>(plane + w) = PK::pack(o.v.y, nxt);
+               else plane[w] = S::from_shifted(o.v.y);                 // the other half is the next warp's
+               if (lane == 0) plane[chk(p, t + (ex == 1 ? 1 : -1))] = S::from_shifted(o.v.x);   // the previous warp's
+             }
+           });
+  if (ACC) {
+    const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
+    *reinterpret_cast<double2 *>(p.accp(0) + c) = make_double2(v0.x + (double)rho.v.x, v0.y + (double)rho.v.y);
+    *reinterpret_cast<double2 *>(p.accp(1) + c) = make_double2(v1.x + (double)ux.v.x, v1.y + (double)ux.v.y);
+    *reinterpret_cast<double2 *>(p.accp(2) + c) = make_double2(v2.x + (double)uy.v.x, v2.y + (double)uy.v.y);
+    *reinterpret_cast<double2 *>(p.accp(3) + c) = make_double2(v3.x + (double)uz.v.x, v3.y + (double)uz.v.y);
+  }
+}
+
+// Grid: (ceil(pitch / 64), ceil(ny / WY), nz); warp = two adjacent row segments.
+template <int DT, bool ODD, bool ACC, typename Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
+    k_step_aa_pair(const __grid_constant__ StepParams p, AAParams a) {
+  const Geom &g = p.g;
+  const int y = blockIdx.y * Cfg::WY + threadIdx.y;
+  if (y >= g.ny) return;
+  const int z = blockIdx.z, lane = threadIdx.x, bx = blockIdx.x;
+  const int sa = 2 * bx;
+  const int seg = (z * g.ny + y) * g.nseg_x + sa;
+  const uint8_t ka = __ldg(p.tiles + seg);
+  const uint8_t kb = sa + 1 < g.nseg_x ? __ldg(p.tiles + seg + 1) : (uint8_t)TILE_ALL_SOLID;
+  if (ka & kb & TILE_ALL_SOLID) return;
+  const int x0s = 2 * SEG * bx, x0 = x0s + 2 * lane;
+  if (!((ka | kb) & TILE_CHECK)) {
+    if (!ODD) {
+      aa_pair_even_fast<DT, ACC>(p, x0, y, z);
+      return;
+    }
+    if (x0s > 0 && x0s + 2 * SEG < g.nx && z < g.nz - 1) {           // uniform across the warp
+      aa_pair_odd_interior<DT, ACC>(p, x0, y, z, lane);
+      return;
+    }
+    float fxw = 0.0f, fzw = 0.0f;                                    // inlet, outlet, top: per cell
+    int hit = 0;
+    if (x0 < g.nx) aa_odd_cell<DT, false, ACC>(p, a, x0, y, z, fxw, fzw, hit);
+    if (x0 + 1 < g.nx) aa_odd_cell<DT, false, ACC>(p, a, x0 + 1, y, z, fxw, fzw, hit);
+    return;
+  }
+  float fxw = 0.0f, fzw = 0.0f;
+  int hit = 0;
+  if (ODD) {
+    if (x0 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0, y, z, fxw, fzw, hit);
+    if (x0 + 1 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0 + 1, y, z, fxw, fzw, hit);
+  } else {
+    if (x0 < g.nx) aa_even_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
+    if (x0 + 1 < g.nx) aa_even_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
+  }
+  if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+}
+
 // One AA step.  odd: reads natural planes, writes slot s to plane opp(s);
 // even: reads slot s from plane opp(s), writes S_k to plane k.
 template <int DT>
@@ -311,6 +462,19 @@ cudaError_t launch_aa(const StepParams &p_in, const AAParams &a, bool odd, cudaS
     k_aa_ghost<DT><<<gg, 128, 0, s>>>(p, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+  }
+  if constexpr (is16(DT)) {                          // two cells per thread
+    using Cfg = StepCfg<4, 8>;
+    const dim3 grid((unsigned)((p.g.nseg_x + 1) / 2), (unsigned)((p.g.ny + Cfg::WY - 1) / Cfg::WY), (unsigned)p.g.nz);
+    const dim3 block(32, Cfg::WY);
+    if (odd) {
+      if (p.acc) k_step_aa_pair<DT, true, true, Cfg><<<grid, block, 0, s>>>(p, a);
+      else k_step_aa_pair<DT, true, false, Cfg><<<grid, block, 0, s>>>(p, a);
+    } else {
+      if (p.acc) k_step_aa_pair<DT, false, true, Cfg><<<grid, block, 0, s>>>(p, a);
+      else k_step_aa_pair<DT, false, false, Cfg><<<grid, block, 0, s>>>(p, a);
+    }
+    return cudaGetLastError();
   }
   auto go = [&](auto cfg) -> cudaError_t {
     using Cfg = decltype(cfg);

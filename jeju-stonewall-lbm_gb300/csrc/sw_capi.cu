@@ -42,6 +42,11 @@ bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 cudaStream_t st(sw_stream s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Clears the calling thread's last CUDA error before this library launches, so
+// that the error read after the launch is the launch's own and not one an
+// earlier, unrelated runtime call (in the caller or another library) left behind.
+void clear_stale() { (void)cudaGetLastError(); }
+
 }  // namespace
 
 namespace sw {
@@ -94,33 +99,39 @@ size_t sw_dtype_size(int dtype) {
 
 int sw_pack_flag(const sw_geom *g, const uint8_t *flag_ref, uint8_t *flag, sw_stream s) {
   if (!geom_ok(g) || !flag_ref || !flag) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_pack_flag(to_geom(g), flag_ref, flag, st(s)));
 }
 
 int sw_pack_f(const sw_geom *g, int dtype, int ref_dtype, const void *f_ref, void *f, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || (ref_dtype != SW_F32 && ref_dtype != SW_F64) || !f_ref || !f)
     return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_pack_f(to_geom(g), dtype, ref_dtype, f_ref, f, st(s)));
 }
 
 int sw_unpack_f(const sw_geom *g, int dtype, int ref_dtype, const void *f, void *f_ref, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || (ref_dtype != SW_F32 && ref_dtype != SW_F64) || !f_ref || !f)
     return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_unpack_f(to_geom(g), dtype, ref_dtype, f, f_ref, st(s)));
 }
 
 int sw_unpack_u(const sw_geom *g, const float *u, float *u_ref, sw_stream s) {
   if (!geom_ok(g) || !u || !u_ref) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_unpack_u(to_geom(g), u, u_ref, st(s)));
 }
 
 int sw_unpack_acc(const sw_geom *g, const double *acc, double *acc_ref, sw_stream s) {
   if (!geom_ok(g) || !acc || !acc_ref) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_unpack_acc(to_geom(g), acc, acc_ref, st(s)));
 }
 
 int sw_build_tiles(const sw_geom *g, const uint8_t *flag, uint8_t *tiles, sw_stream s) {
   if (!geom_ok(g) || !flag || !tiles) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_build_tiles(to_geom(g), flag, tiles, st(s)));
 }
 
@@ -128,6 +139,7 @@ int sw_init(const sw_geom *g, int dtype, void *f, const uint8_t *flag, const flo
             int32_t noise_kind, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !uin || !aligned16(f)) return SW_ERR_BAD_ARG;
   if (noise_kind != SW_NOISE_UNIFORM && noise_kind != SW_NOISE_GAUSSIAN) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_init(to_geom(g), dtype, f, flag, uin, noise, seed, noise_kind, st(s)));
 }
 
@@ -168,6 +180,7 @@ int step_impl(const sw_geom *g, int dtype, const void *f_in, void *f_out, const 
   p.status = status;
   p.cfg = cfg;
   p.tma_poll_limit = g_tma_poll_limit;
+  clear_stale();
   cudaError_t e;
   switch (dtype) {
     case SW_F32: e = sw::step_f32(p, st(s)); break;
@@ -252,17 +265,20 @@ int sw_get_step_config_accum(int dtype) { return dtype_ok(dtype) ? g_step_cfg_ac
 
 int sw_macro(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !u) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_macro(to_geom(g), dtype, f, flag, u, nullptr, st(s)));
 }
 
 int sw_accum(const sw_geom *g, const float *u, double *acc, sw_stream s) {
   if (!geom_ok(g) || !u || !acc) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_accum(to_geom(g), u, acc, st(s)));
 }
 
 int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *flag, float *u, double *acc,
                    sw_stream s) {
   if (!geom_ok(g) || !dtype_ok(dtype) || !f || !flag || !acc) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_macro(to_geom(g), dtype, f, flag, u, acc, st(s)));
 }
 
@@ -312,6 +328,7 @@ int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_de
   if (!hdr_dev || !table_dev || !dtype_ok(dtype) || k < 0) return SW_ERR_BAD_ARG;
   if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
   if (!sw::batch_config_valid(dtype, cfg)) return SW_ERR_UNSUPPORTED;
+  clear_stale();
   cudaError_t e;
   switch (dtype) {
     case SW_F32: e = sw::batch_f32(hdr_dev, table_dev, cfg, k, st(s)); break;
@@ -347,6 +364,7 @@ int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t 
   p.cfg = 0;
   p.tma_poll_limit = g_tma_poll_limit;
   sw::AAParams a{ghost, ghost};
+  clear_stale();
   cudaError_t e;
   switch (dtype) {
     case SW_F32: e = sw::aa_f32(p, a, odd != 0, st(s)); break;
@@ -359,6 +377,7 @@ int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t 
 
 int sw_force_to_f64(const int64_t *force, double *out, int64_t n, sw_stream s) {
   if (n < 0 || (n > 0 && (!force || !out))) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_force_to_f64(reinterpret_cast<const long long *>(force), out, n, st(s)));
 }
 
@@ -368,21 +387,25 @@ int sw_coefficients(const int64_t *force, int64_t n_steps, int32_t nz, double UH
   if (n_steps > 0 && (!force || !coef || ((uintptr_t)force & 15u))) return SW_ERR_BAD_ARG;
   const double qref = 0.5 * (UH * UH);
   const double qa = qref * (H * (double)ny);
+  clear_stale();
   return cuda_status(sw::aux_coefficients(reinterpret_cast<const long long *>(force), n_steps, nz, qa, H, coef, st(s)));
 }
 
 int sw_coef_stats(const double *coef, int64_t n_steps, int64_t n_spin, double *stats, sw_stream s) {
   if (n_steps < 0 || n_spin < 0 || !stats || (n_steps > 0 && !coef)) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_coef_stats(coef, n_steps, n_spin, stats, st(s)));
 }
 
 int sw_slice_xz(const sw_geom *g, const float *u, int32_t y0, float *out, sw_stream s) {
   if (!geom_ok(g) || !u || !out || y0 < 0 || y0 >= g->ny) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_slice_xz(to_geom(g), u, y0, out, st(s)));
 }
 
 int sw_slice_xy(const sw_geom *g, const float *u, int32_t z0, float *out, sw_stream s) {
   if (!geom_ok(g) || !u || !out || z0 < 0 || z0 >= g->nz) return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_slice_xy(to_geom(g), u, z0, out, st(s)));
 }
 
@@ -392,6 +415,7 @@ int sw_qcoarse(const sw_geom *g, const float *u, const uint8_t *flag, int32_t x0
   // every cell a block visits, and its +-1 neighbours in x and z, lies inside the grid
   if ((long long)x0 + (long long)di * ds > g->nx || (long long)dj * ds > g->ny || (long long)dk * ds > g->nz)
     return SW_ERR_BAD_ARG;
+  clear_stale();
   return cuda_status(sw::aux_qcoarse(to_geom(g), u, flag, x0, ds, di, dj, dk, out, st(s)));
 }
 

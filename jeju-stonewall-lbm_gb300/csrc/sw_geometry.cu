@@ -171,6 +171,7 @@ int sw_pack_ellipsoids(const sw_ellipsoid *cand, int32_t n, int32_t X0, int32_t 
   if (n < 0 || (n > 0 && !cand) || !box_bits || !state || X0 < 0 || T <= 0 || ny <= 0 || z_hi < 2)
     return SW_ERR_BAD_ARG;
   if (sw::pack_box_bytes(T, ny, z_hi) > sw::kPackBoxBytesMax) return SW_ERR_TOO_LARGE;
+  (void)cudaGetLastError();                                         // report this launch's error only
   const cudaError_t e = sw::launch_pack_ellipsoids(cand, n, X0, T, ny, z_hi, target, box_bits,
                                                    reinterpret_cast<long long *>(state),
                                                    reinterpret_cast<cudaStream_t>(s));
@@ -185,6 +186,7 @@ int64_t sw_pack_box_bytes(int32_t T, int32_t ny, int32_t z_hi) {
 int sw_voxelize_stones(const sw_stone *stones, int32_t n, int32_t nx, int32_t ny, int32_t nz, uint8_t *mask,
                        int32_t *amb, int32_t cap, sw_stream s) {
   if (n < 0 || (n > 0 && !stones) || !mask || !amb || cap < 0 || nx <= 0 || ny <= 0 || nz <= 0) return SW_ERR_BAD_ARG;
+  (void)cudaGetLastError();
   const cudaError_t e = sw::launch_voxelize_stones(stones, n, nx, ny, nz, mask, amb, cap,
                                                    reinterpret_cast<cudaStream_t>(s));
   return e == cudaSuccess ? SW_OK : sw::note_cuda_error((int)e);

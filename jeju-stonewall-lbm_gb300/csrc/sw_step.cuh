@@ -107,6 +107,20 @@ template <typename R, typename Ctx> __device__ __forceinline__ Phys<R> phys(cons
 template <typename Ctx> __device__ __forceinline__ void note_status(const Ctx &p, unsigned int bits) {
   if (p.status != nullptr) atomicOr(p.status, bits);
 }
+// Element offset within a population plane (also the flag, tiles and sums
+// planes).  The bounds-checked build (-DSW_CHECK, libstonewall_check.so) tests
+// every computed offset against the plane and, outside it, reports
+// SW_STATUS_BOUNDS and uses offset 0 instead; the normal build only passes it on.
+template <typename Ctx> __device__ __forceinline__ int chk(const Ctx &p, int off) {
+#ifdef SW_CHECK
+  if ((unsigned long long)(long long)off >= (unsigned long long)p.g.plane) {
+    note_status(p, SW_STATUS_BOUNDS);
+    return 0;
+  }
+#endif
+  return off;
+}
+
 // |v| <= largest finite value: false for infinities and NaN.
 __device__ __forceinline__ bool finite_val(float v) { return fabsf(v) <= 3.402823466e38f; }
 __device__ __forceinline__ bool finite_val(double v) { return fabs(v) <= 1.7976931348623157e308; }
@@ -226,10 +240,13 @@ template <int WY_, int MINB_> struct StepCfg {
 // two cells per thread with TMA-staged sources (16-bit storage only), see sw_tma.cuh:
 // (id, row-groups per block, stages, resident blocks asked of the register allocator).
 // Shared memory holds a 2-stage block to 7 resident blocks (4 on accumulating
-// steps), so 11-13 give the registers that residency leaves (72 and 128 per thread).
-#define SW_TMA_CONFIGS(X) X(8, 4, 2, 8) X(9, 2, 2, 8) X(10, 4, 2, 10) X(11, 4, 2, 7) X(12, 2, 2, 7) X(13, 4, 2, 4) \
-  X(14, 4, 3, 5)
-constexpr int kStepConfigs = 15;
+// steps), so 12 and 13 give the registers that residency leaves (72 and 128 per
+// thread).  One item per block (one stage, no block barrier) leaves shared
+// memory for more blocks: 10, 11 and 14-17 trade registers for residency
+// (measured at 800x160x160: 16 fastest plain, 15 fastest accumulating).
+#define SW_TMA_CONFIGS(X) X(8, 4, 2, 8) X(9, 2, 2, 8) X(10, 1, 1, 9) X(11, 1, 1, 7) X(12, 2, 2, 7) X(13, 4, 2, 4) \
+  X(14, 1, 1, 12) X(15, 1, 1, 8) X(16, 1, 1, 10) X(17, 1, 1, 6)
+constexpr int kStepConfigs = 18;
 
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
 // tests (segments next to stones, the ground or a fluid cell at z = 0).
@@ -241,7 +258,7 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
   using T = typename S::T;
   using R = typename S::R;
   const Geom &g = p.g;
-  const int c = (z * g.ny + y) * g.pitch + x;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x);
   auto in = [&](int pop) { return p.template in<T>(pop); };
   auto out = [&](int pop) { return p.template out<T>(pop); };
   if (CHECK && p.flag[c] != 0) return;                          // lbm3d.py:65-66
@@ -284,8 +301,8 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
   static_for<0, Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
     constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
-    const int src = (ex == 1 ? off_xm : ex == -1 ? off_xp : c) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
-                    (ez == 1 ? off_zm : ez == -1 ? off_zp : 0);
+    const int src = chk(p, (ex == 1 ? off_xm : ex == -1 ? off_xp : c) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
+                               (ez == 1 ? off_zm : ez == -1 ? off_zp : 0));
     bool pull = true;
     if constexpr (CHECK) {
       // a source below z = 0 (only for a fluid cell in the bottom plane, which
@@ -567,7 +584,7 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
   const bool has_b = x0 + 1 < g.nx;   // cell x0 + 1 exists
   const bool has_r = x0 + 2 < g.nx;   // cell x0 + 2 exists (else the outlet copies x0 + 1)
   const bool inlet = x0 == 0;         // cell x0 is the inlet
-  const int c = (z * g.ny + y) * g.pitch + x0;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
   auto in = [&](int pop) { return p.template in<T>(pop); };
   const int row = g.pitch, lev = g.ny * g.pitch;
   const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
@@ -582,10 +599,11 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
     constexpr int i = decltype(I)::value;
     constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
     const int rowoff = (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) + (ez == 1 ? off_zm : ez == -1 ? off_zp : 0);
-    const T *base = ((ez == -1 && top) ? in(MIRZ(i)) : in(i)) + (c + rowoff);   // source row, column x0
-    P[i] = live ? __ldg(reinterpret_cast<const unsigned int *>(base)) : 0u;
-    if constexpr (ex == 1) edge[i] = (lane == 0 && live && x0 > 0) ? PK::one(base - 1) : 0.0f;
-    if constexpr (ex == -1) edge[i] = (lane == 31 && live && has_r) ? PK::one(base + 2) : 0.0f;
+    const T *plane = (ez == -1 && top) ? in(MIRZ(i)) : in(i);
+    const int src = c + rowoff;                                       // source row, column x0
+    P[i] = live ? __ldg(reinterpret_cast<const unsigned int *>(plane + chk(p, src))) : 0u;
+    if constexpr (ex == 1) edge[i] = (lane == 0 && live && x0 > 0) ? PK::one(plane + chk(p, src - 1)) : 0.0f;
+    if constexpr (ex == -1) edge[i] = (lane == 31 && live && has_r) ? PK::one(plane + chk(p, src + 2)) : 0.0f;
   });
   // accumulation steps: the sums of both cells, read with the populations
   double2 acc_old[4];

@@ -22,11 +22,11 @@
 // is -1 or ny reads a one-row box of row ny - 1 or 0 loaded beside the stage.
 //
 // A block runs ITEMS consecutive y row-groups of one 64-cell x segment pair at
-// one level, with NSTAGE stages in flight (measured at c2: 4 row-groups and 2
-// stages beat 1, 2, 8 and 16 row-groups, 3 stages, and a variant with a
-// producer warp releasing stages through mbarriers instead of a block barrier).  Every wait on an mbarrier is
-// bounded; on time-out the block records the event in g_tma_timeouts, waits
-// (bounded) for its copies in flight and leaves.
+// one level, with NSTAGE stages in flight.  When ITEMS > NSTAGE the stages form a
+// ring released by a block barrier per item; otherwise every item is issued at
+// the start and the warps run without barriers.  Every wait on an mbarrier is
+// bounded; on time-out the block records the event in g_tma_timeouts and the
+// lattice's status word, waits (bounded) for its copies in flight and leaves.
 #pragma once
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -147,7 +147,7 @@ __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t
   const bool has_b = INTERIOR || x0 + 1 < g.nx;
   const bool has_r = INTERIOR || x0 + 2 < g.nx;
   const bool inlet = !INTERIOR && x0 == 0;
-  const int c = (z * g.ny + y) * g.pitch + x0;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
   const int lane_word = 4 + lane;                                     // 32-bit word of elements 8 + 2 lane, + 1
   f2 v[Q];
   static_for<0, Q>([&](auto I) {
@@ -184,6 +184,9 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     k_step_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap map1,
                const __grid_constant__ CUtensorMap map_acc, const __grid_constant__ StepParams p) {
   constexpr int kStage = tma_stage_bytes<ACC>();
+  // With no more items than stages every item's copies are issued at the start
+  // and no stage is reused: warps then run their items without block barriers.
+  constexpr bool kRing = Cfg::ITEMS > Cfg::NSTAGE;
   static_assert(2 * Cfg::ITEMS <= 32, "one lane per tile byte of the block's items");
   extern __shared__ __align__(128) uint8_t smem_raw[];
   __shared__ __align__(8) unsigned long long bars[Cfg::NSTAGE];
@@ -241,16 +244,23 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
         if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
       }
     }
-    ok = __syncthreads_and(ok);                                       // stage s is free again
-    if (!ok) break;
-    if (leader && j + Cfg::NSTAGE < n_items)
-      tma_issue<ACC>(&map, &map1, &map_acc, g, x0s, (yb0 + j + Cfg::NSTAGE) * 4, z, st, smem_u32(&bars[s]));
+    if constexpr (kRing) {                                            // stages are reused: the block
+      ok = __syncthreads_and(ok);                                     // barrier frees stage s
+      if (!ok) break;
+      if (leader && j + Cfg::NSTAGE < n_items)
+        tma_issue<ACC>(&map, &map1, &map_acc, g, x0s, (yb0 + j + Cfg::NSTAGE) * 4, z, st, smem_u32(&bars[s]));
+    }
   }
-  if (!ok && leader) {                                                // item j failed: items j .. j+NSTAGE-1
-    atomicAdd(&g_tma_timeouts, 1u);                                   // were issued; let their copies land
-    note_status(p, SW_STATUS_TIMEOUT);                                // (with the normal bound)
-    for (int k = j; k < n_items && k < j + Cfg::NSTAGE; ++k)
-      (void)mbar_wait(smem_u32(&bars[k % Cfg::NSTAGE]), (uint32_t)((k / Cfg::NSTAGE) & 1));
+  if constexpr (!kRing) ok = __syncthreads_and(ok);                 // every item was issued at the start
+  if (!ok && leader) {                                                // some wait gave up: let every copy
+    atomicAdd(&g_tma_timeouts, 1u);                                   // in flight land (normal bound)
+    note_status(p, SW_STATUS_TIMEOUT);
+    if constexpr (kRing) {                                            // item j failed: j .. j+NSTAGE-1 issued
+      for (int k = j; k < n_items && k < j + Cfg::NSTAGE; ++k)
+        (void)mbar_wait(smem_u32(&bars[k % Cfg::NSTAGE]), (uint32_t)((k / Cfg::NSTAGE) & 1));
+    } else {
+      for (int k = 0; k < n_items; ++k) (void)mbar_wait(smem_u32(&bars[k]), 0u);
+    }
   }
 }
 

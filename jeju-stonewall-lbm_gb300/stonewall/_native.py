@@ -67,10 +67,17 @@ def lib():
     if not os.path.exists(LIB_PATH):
         raise NativeUnavailable(f"{LIB_PATH} is not built; run `python -m stonewall.build` "
                                 "(there is no CPU fallback)")
+    _lib = load(LIB_PATH)
+    return _lib
+
+
+def load(path):
+    """A CDLL of the library at path (the product library, or the bounds-checked build) with the
+    argument and result types of every entry point set."""
     try:
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(path)
     except OSError as e:
-        raise NativeUnavailable(f"cannot load {LIB_PATH}: {e}") from e
+        raise NativeUnavailable(f"cannot load {path}: {e}") from e
     P, G = ctypes.c_void_p, ctypes.POINTER(SwGeom)
     i32, i64, f32, f64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_double
     sig = {
@@ -121,7 +128,6 @@ def lib():
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
         fn.argtypes, fn.restype = args, res
-    _lib = L
     return L
 
 

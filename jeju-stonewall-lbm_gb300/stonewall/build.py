@@ -1,6 +1,12 @@
 """Compile the CUDA sources in ../csrc into the in-tree shared library libstonewall.so.
 
     python -m stonewall.build            (from jeju-stonewall-lbm_gb300/)
+    python -m stonewall.build --check    the bounds-checked build, libstonewall_check.so
+
+The bounds-checked build compiles the same sources with -DSW_CHECK: every
+computed element offset of the step kernels is tested against its plane and an
+offset outside it is reported in the lattice's status word (SW_STATUS_BOUNDS)
+instead of being used.  It is for tests; the product loads libstonewall.so.
 
 One nvcc process per translation unit, run in parallel, then one link.  Only
 sm_103a (GB300) code is generated.  The object files go to _build/ beside this
@@ -19,6 +25,7 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libstonewall.so")
+LIB_CHECK = os.path.join(HERE, "libstonewall_check.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -44,9 +51,9 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
-def _compile(src, verbose):
-    obj = os.path.join(BUILD, src[:-3] + ".o")
-    cmd = [nvcc()] + ARCH + COMMON + (["--fmad=false"] if src in NO_FMAD else [])
+def _compile(src, verbose, check=False):
+    obj = os.path.join(BUILD, ("check_" if check else "") + src[:-3] + ".o")
+    cmd = [nvcc()] + ARCH + COMMON + (["--fmad=false"] if src in NO_FMAD else []) + (["-DSW_CHECK"] if check else [])
     if verbose:
         cmd += ["-Xptxas", "-v"]
     cmd += ["-c", os.path.join(CSRC, src), "-o", obj]
@@ -56,23 +63,24 @@ def _compile(src, verbose):
     return obj, r.stderr
 
 
-def build(force=False, verbose=False):
-    """Build libstonewall.so if any source is newer than it; returns its path."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
-        return LIB
+def build(force=False, verbose=False, check=False):
+    """Build libstonewall.so (check: libstonewall_check.so) if any source is newer than it; returns its path."""
+    lib = LIB_CHECK if check else LIB
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _deps():
+        return lib
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        results = list(ex.map(lambda s: _compile(s, verbose), srcs))
+        results = list(ex.map(lambda s: _compile(s, verbose, check), srcs))
     if verbose:
         for (_, log), s in zip(results, srcs):
             print(f"== {s}\n{log}")
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + ["-lcudart"]
     subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, check="--check" in sys.argv))
