@@ -248,12 +248,29 @@ template <int WY_, int MINB_> struct StepCfg {
   X(14, 1, 1, 12) X(15, 1, 1, 8) X(16, 1, 1, 10) X(17, 1, 1, 6)
 constexpr int kStepConfigs = 18;
 
+// Pulled value of the link of population I, whose source is element offset src
+// of plane P (P = I, or its z mirror at the top), read from the lattice.
+template <int DT> struct GlobalPull {
+  template <int I, int P, typename Ctx>
+  __device__ __forceinline__ typename Store<DT>::R operator()(Int<I>, Int<P>, const Ctx &p, int src) const {
+    return Store<DT>::template ld<P>(p.template in<typename Store<DT>::T>(P) + src);
+  }
+};
+
 // One cell of the pull-scheme step.  CHECK selects the path with neighbour flag
 // tests (segments next to stones, the ground or a fluid cell at z = 0).
 // Offsets within a population plane are 32-bit (grids below 2^31 cells).
 template <int DT, bool CHECK, bool ACC, typename Ctx>
 __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typename Store<DT>::R &fxw,
                                           typename Store<DT>::R &fzw, int &hit) {
+  step_cell<DT, CHECK, ACC>(p, x, y, z, fxw, fzw, hit, GlobalPull<DT>{});
+}
+
+// The same with the pulled values from `pull` (the TMA-staged step reads them
+// from its shared-memory boxes); bounce-back values are read from the lattice.
+template <int DT, bool CHECK, bool ACC, typename Ctx, typename Pull>
+__device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typename Store<DT>::R &fxw,
+                                          typename Store<DT>::R &fzw, int &hit, const Pull &pull_val) {
   using S = Store<DT>;
   using T = typename S::T;
   using R = typename S::R;
@@ -322,10 +339,10 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
     }
     if (pull) {                                                 // lbm3d.py:97
       if constexpr (ez == -1) {
-        if (top) fl[i] = S::template ld<MIRZ(i)>(in(MIRZ(i)) + src);
-        else fl[i] = S::template ld<i>(in(i) + src);
+        if (top) fl[i] = pull_val(Int<i>{}, Int<MIRZ(i)>{}, p, src);
+        else fl[i] = pull_val(Int<i>{}, Int<i>{}, p, src);
       } else {
-        fl[i] = S::template ld<i>(in(i) + src);
+        fl[i] = pull_val(Int<i>{}, Int<i>{}, p, src);
       }
     }
   });

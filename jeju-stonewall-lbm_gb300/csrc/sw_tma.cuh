@@ -178,6 +178,29 @@ __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t
   pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_box[k * 4 * 32]; });
 }
 
+// The checked path's pulled values from the staged boxes: the box of the link's
+// population holds its source row (the z mirror at the top, the periodic wrap
+// rows beside the stage), x from x0s - 8; the outlet copies column x.
+template <int DT> struct TmaPull {
+  const uint8_t *st;
+  int xl;        // x - x0s
+  int x, y, w;
+  const Geom &g;
+  template <int I, int P, typename Ctx>
+  __device__ __forceinline__ float operator()(Int<I>, Int<P>, const Ctx &, int) const {
+    using T = typename Store<DT>::T;
+    constexpr int ex = CX(I), ey = CY(I);
+    const uint8_t *rowp = st + I * kTmaBoxBytes + w * kTmaRowBytes;
+    if constexpr (ey == 1) {
+      if (y == 0) rowp = st + Q * kTmaBoxBytes + wrap_slot(I) * kTmaWrapBytes;
+    } else if constexpr (ey == -1) {
+      if (y == g.ny - 1) rowp = st + Q * kTmaBoxBytes + wrap_slot(I) * kTmaWrapBytes;
+    }
+    const int e = (ex == -1 && x + 1 >= g.nx) ? xl + 8 : xl + 8 - ex;
+    return Store<DT>::to_shifted(reinterpret_cast<const T *>(rowp)[e]);
+  }
+};
+
 // Grid: (ceil(pitch / 64), ceil(ceil(ny / 4) / ITEMS), nz); block = 4 warps, warp w = row y0 + w.
 template <int DT, bool ACC, typename Cfg>
 __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
@@ -237,10 +260,13 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
         else
           tma_pair_fast<DT, ACC, false>(p, smem + s * kStage, x0, y, z, w, lane);
       } else {                                                        // next to stones / ground: per cell
-        float fxw = 0.0f, fzw = 0.0f;
+        float fxw = 0.0f, fzw = 0.0f;                                 // (sources from the staged boxes)
         int hit = 0;
-        if (x0 < g.nx) step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
-        if (x0 + 1 < g.nx) step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
+        const uint8_t *stp = smem + s * kStage;
+        if (x0 < g.nx)
+          step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit, TmaPull<DT>{stp, 2 * lane, x0, y, w, g});
+        if (x0 + 1 < g.nx)
+          step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit, TmaPull<DT>{stp, 2 * lane + 1, x0 + 1, y, w, g});
         if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
       }
     }
