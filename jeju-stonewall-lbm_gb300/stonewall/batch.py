@@ -27,6 +27,7 @@ import ctypes
 import torch
 
 from . import _native as N
+from . import trace
 from .fields import StatusWord, _stream
 
 
@@ -245,10 +246,12 @@ class Batch:
             if not live:
                 return self
             if graph_mode:
-                self._graph_run(slot, len(live), c)
+                with trace.range(f"batch graph chunk ({len(live)} walls, {c} steps)"):
+                    self._graph_run(slot, len(live), c)
                 self.launches += sum(min(c, m.n_total - m.t) for m in live)
             elif use_graphs and c == self.chunk:
-                self._graph(c).replay()
+                with trace.range(f"batch persistent chunk ({len(live)} walls, {c} steps)"):
+                    self._graph(c).replay()
                 self.launches += c
             else:
                 for k in range(c):

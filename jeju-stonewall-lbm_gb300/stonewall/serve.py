@@ -45,6 +45,7 @@ from .batch import Batch
 from .geometry import ellipsoid_wall
 from .metrics import coefficients, device_stats, stats
 from .params import baseline_params, flags_from_wall
+from . import trace
 from .solver import DeviceWaitTimeout, Diverged, WallSolver
 
 DTYPE_BYTES = {"f32": 4, "f16": 2, "bf16": 2, "f64": 8}
@@ -243,7 +244,8 @@ class Server:
                 queue.append(reqs[i])
                 prepared[reqs[i].rid] = self.pool.submit(self._prepare, reqs[i])
                 i += 1
-            self._admit(queue, prepared, now)
+            with trace.range("server admit"):
+                self._admit(queue, prepared, now)
             active = [b for b in self.batches.values() if b.pending()]
             self.max_used = max(self.max_used, self.used)
             if active:
@@ -256,9 +258,11 @@ class Server:
                     break
                 time.sleep(0.005)
             if self.check_every and it % self.check_every == 0 and self.resident:
-                self._check_residents()
+                with trace.range("server status check"):
+                    self._check_residents()
             now = self.clock() - t0
-            self._retire(now)
+            with trace.range("server retire"):
+                self._retire(now)
             if max_seconds is not None and now > max_seconds and not drain:
                 break
             if max_seconds is not None and now > max_seconds and drain and i < len(reqs):

@@ -26,6 +26,7 @@ import torch
 
 from . import _native as N
 from . import kernels as K
+from . import trace
 from .fields import Accum, Flags, ForceSeries, Grid, Lattice, Macro, StatusWord
 
 
@@ -209,7 +210,8 @@ class WallSolver:
             if use_graphs and n >= c and same_side and (self.pattern == "ab" or self.aa_odd_next):
                 phase = (t - self.n_spin) % self.acc_every if t >= self.n_spin else None
                 graph, n_acc = self._graph_for((c, self.cur, phase))
-                graph.replay()
+                with trace.range(f"solver chunk t={t}"):
+                    graph.replay()
                 self.force.data[t:t + c].copy_(self._ring.data)
                 self.cur ^= (c & 1) if self.pattern == "ab" else 0
                 self.t += c
