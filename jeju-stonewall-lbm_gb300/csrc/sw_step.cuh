@@ -248,12 +248,31 @@ template <int WY_, int MINB_> struct StepCfg {
   X(14, 1, 1, 12) X(15, 1, 1, 8) X(16, 1, 1, 10) X(17, 1, 1, 6)
 constexpr int kStepConfigs = 18;
 
-// Pulled value of the link of population I, whose source is element offset src
-// of plane P (P = I, or its z mirror at the top), read from the lattice.
+// Where the checked path of step_cell takes its inputs from, read from the
+// lattice and the flags:
+//   operator()  the pulled value of the link of population I, whose source is
+//               element offset src of plane P (P = I, or its z mirror at the top);
+//   self_solid  whether cell c itself is not fluid;
+//   src_flag    the flag of link I's source (0 fluid, SW_WALL, SW_GROUND); a
+//               source below z = 0 (only for a fluid cell in the bottom plane,
+//               which the reference never has) is treated as ground;
+//   bounce      the half-way bounce-back value of link I: the cell's own
+//               population OPP(I) (lbm3d.py:89-95).
 template <int DT> struct GlobalPull {
+  using R = typename Store<DT>::R;
+  using T = typename Store<DT>::T;
   template <int I, int P, typename Ctx>
-  __device__ __forceinline__ typename Store<DT>::R operator()(Int<I>, Int<P>, const Ctx &p, int src) const {
-    return Store<DT>::template ld<P>(p.template in<typename Store<DT>::T>(P) + src);
+  __device__ __forceinline__ R operator()(Int<I>, Int<P>, const Ctx &p, int src) const {
+    return Store<DT>::template ld<P>(p.template in<T>(P) + src);
+  }
+  template <typename Ctx> __device__ __forceinline__ bool self_solid(const Ctx &p, int c) const {
+    return p.flag[c] != 0;
+  }
+  template <int I, typename Ctx> __device__ __forceinline__ uint8_t src_flag(Int<I>, const Ctx &p, int src, int z) const {
+    return (CZ(I) == 1 && z == 0) ? (uint8_t)SW_GROUND : __ldg(p.flag + src);
+  }
+  template <int I, typename Ctx> __device__ __forceinline__ R bounce(Int<I>, const Ctx &p, int c) const {
+    return Store<DT>::template ld<OPP(I)>(p.template in<T>(OPP(I)) + c);
   }
 };
 
@@ -266,8 +285,9 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
   step_cell<DT, CHECK, ACC>(p, x, y, z, fxw, fzw, hit, GlobalPull<DT>{});
 }
 
-// The same with the pulled values from `pull` (the TMA-staged step reads them
-// from its shared-memory boxes); bounce-back values are read from the lattice.
+// The same with the checked path's inputs from `pull_val` (the TMA-staged step
+// reads the pulled values from its shared-memory boxes and has the flags and
+// bounce-back values in registers, fetched while its copies were in flight).
 template <int DT, bool CHECK, bool ACC, typename Ctx, typename Pull>
 __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typename Store<DT>::R &fxw,
                                           typename Store<DT>::R &fzw, int &hit, const Pull &pull_val) {
@@ -276,9 +296,8 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
   using R = typename S::R;
   const Geom &g = p.g;
   const int c = chk(p, (z * g.ny + y) * g.pitch + x);
-  auto in = [&](int pop) { return p.template in<T>(pop); };
   auto out = [&](int pop) { return p.template out<T>(pop); };
-  if (CHECK && p.flag[c] != 0) return;                          // lbm3d.py:65-66
+  if (CHECK && pull_val.self_solid(p, c)) return;              // lbm3d.py:65-66
   if (x == 0) {                                                 // inlet, lbm3d.py:67-71
     const R u0 = (R)__ldg(p.uin + z);
     const R usq = u0 * u0;
@@ -322,12 +341,10 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
                                (ez == 1 ? off_zm : ez == -1 ? off_zp : 0));
     bool pull = true;
     if constexpr (CHECK) {
-      // a source below z = 0 (only for a fluid cell in the bottom plane, which
-      // the reference never has) is treated as ground
-      const uint8_t fs = (ez == 1 && z == 0) ? (uint8_t)SW_GROUND : __ldg(p.flag + src);
+      const uint8_t fs = pull_val.src_flag(Int<i>{}, p, src, z);
       if (fs != 0) {                                            // lbm3d.py:89-95
         pull = false;
-        const R val = S::template ld<OPP(i)>(in(OPP(i)) + c);
+        const R val = pull_val.bounce(Int<i>{}, p, c);
         if (fs == SW_WALL) {
           const R fr = S::kShift ? val : val - W<R>(i);   // f - w, the rho = 1 background removed
           if constexpr (ex != 0) fxw = fxw - R(2.0) * fr * R(ex);
