@@ -285,9 +285,8 @@ __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typ
   step_cell<DT, CHECK, ACC>(p, x, y, z, fxw, fzw, hit, GlobalPull<DT>{});
 }
 
-// The same with the checked path's inputs from `pull_val` (the TMA-staged step
-// reads the pulled values from its shared-memory boxes and has the flags and
-// bounce-back values in registers, fetched while its copies were in flight).
+// The same with the checked path's inputs from `pull_val` (GlobalPull: the
+// lattice and the flags).
 template <int DT, bool CHECK, bool ACC, typename Ctx, typename Pull>
 __device__ __forceinline__ void step_cell(const Ctx &p, int x, int y, int z, typename Store<DT>::R &fxw,
                                           typename Store<DT>::R &fzw, int &hit, const Pull &pull_val) {
@@ -556,6 +555,117 @@ template <> struct Pack16<SW_BF16_SHIFT> {
   }
 };
 
+// The link masks of one cell of the checked path, for the flags of its pull
+// sources as step_cell maps them (lbm3d.py:77-95): bit i of `solid` is set when
+// link i's source is not fluid, bit i of `wall` when it is a stone; bit 0 of
+// `solid` marks a cell that is itself not fluid (or lies past the row end).
+// The inlet column pulls nothing.  Every load is issued before any is used.
+template <typename Ctx>
+__device__ __forceinline__ void cell_links(const Ctx &p, int x, int y, int z, uint32_t &solid, uint32_t &wall) {
+  const Geom &g = p.g;
+  solid = 1u;
+  wall = 0u;
+  if (x >= g.nx) return;
+  const int c = chk(p, (z * g.ny + y) * g.pitch + x);
+  const uint8_t own = p.flag[c];
+  if (x > 0) {
+    const int row = g.pitch, lev = g.ny * g.pitch;
+    const int off_xm = c - 1;
+    const int off_xp = (x + 1 >= g.nx) ? c : c + 1;
+    const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
+    const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
+    const int off_zm = -lev;
+    const int off_zp = (z == g.nz - 1) ? 0 : lev;
+    uint8_t fs[Q];
+    static_for<1, Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
+      if (ez == 1 && z == 0) {
+        fs[i] = (uint8_t)SW_GROUND;
+      } else {
+        const int src = chk(p, (ex == 1 ? off_xm : ex == -1 ? off_xp : c) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
+                                   (ez == 1 ? off_zm : ez == -1 ? off_zp : 0));
+        fs[i] = __ldg(p.flag + src);
+      }
+    });
+    uint32_t sm = 0u, wm = 0u;
+    static_for<1, Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      sm |= (fs[i] != 0 ? 1u : 0u) << i;
+      wm |= (fs[i] == SW_WALL ? 1u : 0u) << i;
+    });
+    solid = sm;
+    wall = wm;
+  } else {
+    solid = 0u;
+  }
+  if (own != 0) {
+    solid = 1u;
+    wall = 0u;
+  }
+}
+
+// The checked path of a cell pair, first part: the link masks of cells x0 and
+// x0 + 1 and the bounce-back pairs (the 32-bit pair of population OPP(i) at the
+// pair's own offset) of the links that bounce in either cell.  The input
+// lattice is not written during the step, so the TMA-staged step issues these
+// loads before it waits for its copies and their latency overlaps the copies'.
+template <int DT, typename Ctx>
+__device__ __forceinline__ void pair_links_prefetch(const Ctx &p, int x0, int y, int z, uint32_t (&sm)[2],
+                                                     uint32_t (&wm)[2], uint32_t (&bnc)[Q]) {
+  using T = typename Store<DT>::T;
+  const Geom &g = p.g;
+  cell_links(p, x0, y, z, sm[0], wm[0]);
+  cell_links(p, x0 + 1, y, z, sm[1], wm[1]);
+  const uint32_t any = (sm[0] | sm[1]) & ~1u;                 // no link bit in a lane past the row end
+  const int c = (z * g.ny + y) * g.pitch + x0;                // even: the pair is one aligned 32-bit word
+  static_for<1, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    bnc[i] = ((any >> i) & 1u) ? __ldg(reinterpret_cast<const unsigned int *>(p.template in<T>(OPP(i)) + chk(p, c)))
+                               : 0u;
+  });
+  bnc[0] = 0u;
+}
+
+// The checked path of a cell pair, second part, for link I once its pulled pair
+// vi is built: where the link's source is not fluid the cell takes its own
+// population OPP(I) (half-way bounce-back, lbm3d.py:89-95), and a stone's adds
+// -2 (f - w) c to the wall force (lbm3d.py:99-101); cell x0 before x0 + 1.
+template <int DT, int I>
+__device__ __forceinline__ void pair_link(f2 &vi, const uint32_t (&sm)[2], const uint32_t (&wm)[2], uint32_t b,
+                                          float &fxw, float &fzw, int &hit) {
+  using PK = Pack16<DT>;
+  constexpr int ex = CX(I), ez = CZ(I);
+  const float2 own = PK::both(b);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    if ((sm[h] >> I) & 1u) {
+      const float val = h ? own.y : own.x;
+      if (h) vi.v.y = val;
+      else vi.v.x = val;
+      if ((wm[h] >> I) & 1u) {
+        if constexpr (ex != 0) fxw = fxw - 2.0f * val * (float)ex;
+        if constexpr (ez != 0) fzw = fzw - 2.0f * val * (float)ez;
+        hit = 1;
+      }
+    }
+  }
+}
+
+// The checked path of a cell pair, last part: a cell that is not fluid (bit 0 of
+// its mask; also a cell past the row end) gets the rest state g = 0, so that the
+// pair's collision stays finite, and is not stored.  Returns the cells to store
+// (bit 0: x0, bit 1: x0 + 1).
+__device__ __forceinline__ uint32_t pair_solid_cells(f2 (&v)[Q], const uint32_t (&sm)[2]) {
+  const bool sa = sm[0] & 1u, sb = sm[1] & 1u;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    if (sa) v[i].v.x = 0.0f;
+    if (sb) v[i].v.y = 0.0f;
+  }
+  return (sa ? 0u : 1u) | (sb ? 0u : 2u);
+}
+
 // Collision of a cell pair and its stores.  Both cells of the pair are stored
 // with one 32-bit store even when cell x0 + 1 lies past the row end: that
 // half lands in the row's padding columns (x >= nx), which nothing reads.  The
@@ -563,19 +673,26 @@ template <> struct Pack16<SW_BF16_SHIFT> {
 // overwritten by its equilibrium in a branch only its lane takes.
 // has_b: cell x0 + 1 exists (x0 + 1 < nx).  acc_old(k): the old float64 sums
 // of the pair for sum k (a double2; .y unused without has_b), called where
-// they are added.
-template <int DT, bool ACC, typename Ctx, typename AccOld>
+// they are added.  MASKED (the checked path): only the cells in `keep` (bit 0:
+// x0, bit 1: x0 + 1) are stored and summed; the inlet cell only when kept.
+template <int DT, bool ACC, bool MASKED = false, typename Ctx, typename AccOld>
 __device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q], int x0, int c, int z, bool inlet,
-                                                   bool has_b, AccOld &&acc_old) {
+                                                   bool has_b, AccOld &&acc_old, uint32_t keep = 3u) {
   using S = Store<DT>;
   using T = typename S::T;
   using PK = Pack16<DT>;
   const Phys<float> ph = phys<float>(p);
   f2 rho, ux, uy, uz;
+  if (MASKED) inlet = inlet && (keep & 1u);
   collide2(v, x0, has_b, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz,
            p.status, [&](auto I, f2 o) {
              constexpr int i = decltype(I)::value;
-             __stcs(reinterpret_cast<unsigned int *>(p.template out<T>(i) + c), PK::pack(o.v.x, o.v.y));
+             if (!MASKED || keep == 3u)
+               __stcs(reinterpret_cast<unsigned int *>(p.template out<T>(i) + c), PK::pack(o.v.x, o.v.y));
+             else if (keep == 1u)
+               __stcs(p.template out<T>(i) + c, S::from_shifted(o.v.x));
+             else if (keep == 2u)
+               __stcs(p.template out<T>(i) + c + 1, S::from_shifted(o.v.y));
            });
   float u0 = 0.0f;
   if (inlet) {
@@ -594,7 +711,19 @@ __device__ __forceinline__ void pair_collide_store(const Ctx &p, const f2 (&v)[Q
   if (ACC) {
     const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
     const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
-    if (has_b) {                                        // cells x0, x0 + 1: one 16-byte update per sum
+    if (MASKED && keep != 3u) {                         // one cell of the pair (or none)
+      if (keep == 1u) {
+        __stcs(p.accp(0) + c, acc_old(0).x + ra);
+        __stcs(p.accp(1) + c, acc_old(1).x + xa);
+        __stcs(p.accp(2) + c, acc_old(2).x + ya);
+        __stcs(p.accp(3) + c, acc_old(3).x + za);
+      } else if (keep == 2u) {
+        __stcs(p.accp(0) + c + 1, acc_old(0).y + (double)rho.v.y);
+        __stcs(p.accp(1) + c + 1, acc_old(1).y + (double)ux.v.y);
+        __stcs(p.accp(2) + c + 1, acc_old(2).y + (double)uy.v.y);
+        __stcs(p.accp(3) + c + 1, acc_old(3).y + (double)uz.v.y);
+      }
+    } else if (has_b) {                                 // cells x0, x0 + 1: one 16-byte update per sum
       const double2 v0 = acc_old(0), v1 = acc_old(1), v2 = acc_old(2), v3 = acc_old(3);
       __stcs(reinterpret_cast<double2 *>(p.accp(0) + c), make_double2(v0.x + ra, v0.y + (double)rho.v.y));
       __stcs(reinterpret_cast<double2 *>(p.accp(1) + c), make_double2(v1.x + xa, v1.y + (double)ux.v.y));
@@ -669,6 +798,93 @@ __device__ __forceinline__ void step_pair_fast(const Ctx &p, int x0, int y, int 
   pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_old[k]; });
 }
 
+// The checked two-cell step of a lane (segments next to stones or the ground):
+// step_pair_fast's loads and pulls, then the link masks and bounce-back pairs
+// of pair_links_prefetch replace the pulls of the links whose sources are not
+// fluid, wall links add to fxw / fzw / hit, and cells that are not fluid are
+// not stored; a source below z = 0 is not read.  (A separate copy: sharing one
+// template with the fast path changed the fast path's code and slowed it.)
+template <int DT, bool ACC, typename Ctx>
+__device__ __forceinline__ void step_pair_links(const Ctx &p, int x0, int y, int z, int lane, const uint32_t (&sm)[2],
+                                                const uint32_t (&wm)[2], const uint32_t (&bnc)[Q], float &fxw,
+                                                float &fzw, int &hit) {
+  using T = typename Store<DT>::T;
+  using PK = Pack16<DT>;
+  const Geom &g = p.g;
+  const bool live = x0 < g.nx;        // cell x0 exists; the 32-bit pair lies inside the row
+  const bool has_b = x0 + 1 < g.nx;   // cell x0 + 1 exists
+  const bool has_r = x0 + 2 < g.nx;   // cell x0 + 2 exists (else the outlet copies x0 + 1)
+  const bool inlet = x0 == 0;         // cell x0 is the inlet
+  const int c0 = (z * g.ny + y) * g.pitch + x0;
+  const int c = live ? chk(p, c0) : c0;                             // a lane past the row end uses no offset
+  auto in = [&](int pop) { return p.template in<T>(pop); };
+  const int row = g.pitch, lev = g.ny * g.pitch;
+  const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
+  const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
+  const bool top = (z == g.nz - 1);
+  const int off_zm = -lev;
+  const int off_zp = top ? 0 : lev;
+  // phase 1: every load in flight before the first shuffle consumes one
+  uint32_t P[Q];
+  float edge[Q];                                        // lane 0: cell x0 - 1, lane 31: cell x0 + 2
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
+    const int rowoff = (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) + (ez == 1 ? off_zm : ez == -1 ? off_zp : 0);
+    const T *plane = (ez == -1 && top) ? in(MIRZ(i)) : in(i);
+    const int src = c + rowoff;                                       // source row, column x0
+    const bool ld = live && !(ez == 1 && z == 0);                     // (the ground below z = 0 bounces)
+    P[i] = ld ? __ldg(reinterpret_cast<const unsigned int *>(plane + chk(p, src))) : 0u;
+    if constexpr (ex == 1) edge[i] = (lane == 0 && ld && x0 > 0) ? PK::one(plane + chk(p, src - 1)) : 0.0f;
+    if constexpr (ex == -1) edge[i] = (lane == 31 && ld && has_r) ? PK::one(plane + chk(p, src + 2)) : 0.0f;
+  });
+  // accumulation steps: the sums of both cells, read with the populations
+  double2 acc_old[4];
+  if (ACC) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (live && has_b) acc_old[k] = __ldcs(reinterpret_cast<const double2 *>(p.accp(k) + c));
+      else acc_old[k] = make_double2(live ? __ldcs(p.accp(k) + c) : 0.0, 0.0);
+    }
+  }
+  // phase 2: pulls along x from the neighbouring lanes (outlet copies column x)
+  f2 v[Q];
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = CX(i);
+    const float2 own = PK::both(P[i]);
+    if constexpr (ex == 0) {
+      v[i].v = own;
+    } else if constexpr (ex == 1) {                     // sources x0 - 1, x0
+      const uint32_t prev = __shfl_up_sync(0xffffffffu, P[i], 1);
+      v[i] = F2(lane == 0 ? edge[i] : PK::hi(prev), own.x);
+    } else {                                            // sources x0 + 1, x0 + 2
+      const uint32_t next = __shfl_down_sync(0xffffffffu, P[i], 1);
+      const float right = lane == 31 ? edge[i] : PK::lo(next);
+      v[i] = F2(has_b ? own.y : own.x, has_r ? right : own.y);
+    }
+    if constexpr (i > 0) pair_link<DT, i>(v[i], sm, wm, bnc[i], fxw, fzw, hit);
+  });
+  if (!live) return;
+  const uint32_t keep = pair_solid_cells(v, sm);
+  if (keep == 0u) return;
+  pair_collide_store<DT, ACC, true>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_old[k]; }, keep);
+}
+
+// The checked path of a two-cell warp (segments next to stones or the ground).
+// A separate function: inlined next to the fast path, its masks and bounce-back
+// pairs would set the register allocation of the whole kernel and make the
+// fast path spill.
+template <int DT, bool ACC, typename Ctx>
+__device__ __noinline__ void step_pair_checked(const Ctx &p, int x0, int y, int z, int lane, bool force) {
+  float fxw = 0.0f, fzw = 0.0f;
+  int hit = 0;
+  uint32_t sm[2], wm[2], bnc[Q];
+  pair_links_prefetch<DT>(p, x0, y, z, sm, wm, bnc);
+  step_pair_links<DT, ACC>(p, x0, y, z, lane, sm, wm, bnc, fxw, fzw, hit);
+  if (force && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+}
+
 // One warp, the row segments 2 bx and 2 bx + 1 of (y, z).
 template <int DT, bool ACC, typename Ctx>
 __device__ __forceinline__ void step_pair_segment(const Ctx &p, int bx, int y, int z, int lane) {
@@ -684,11 +900,7 @@ __device__ __forceinline__ void step_pair_segment(const Ctx &p, int bx, int y, i
     step_pair_fast<DT, ACC>(p, x0, y, z, lane);
     return;
   }
-  float fxw = 0.0f, fzw = 0.0f;
-  int hit = 0;
-  if (x0 < g.nx) step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
-  if (x0 + 1 < g.nx) step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
-  if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+  step_pair_checked<DT, ACC>(p, x0, y, z, lane, (ka | kb) & TILE_FORCE);
 }
 
 // Grid: (ceil(pitch / 64), ceil(ny / WY), nz); warp = two adjacent row segments.

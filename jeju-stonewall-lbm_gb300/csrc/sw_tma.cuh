@@ -134,20 +134,25 @@ __device__ __forceinline__ void tma_issue(const CUtensorMap *map, const CUtensor
   if constexpr (ACC) tma_load_4d(st + kTmaStageBytes, map_acc, x0, y0, z, 0, bar);
 }
 
-// The pair-kernel fast path with the sources read from the staged boxes (st: the stage).
+// The pair-kernel two-cell step with the sources read from the staged boxes (st: the stage).
 // INTERIOR: the warp's row is neither the inlet segment pair nor the last one
 // (every lane's cells and right neighbour exist) nor a periodic edge row in y,
 // so no lane needs the inlet, outlet or wrap selects (decided per warp and item).
-template <int DT, bool ACC, bool INTERIOR>
+// CHECKED: as step_pair_fast's (link masks and bounce-back pairs from
+// pair_links_prefetch; the boxes read zeros below z = 0).
+template <int DT, bool ACC, bool INTERIOR, bool CHECKED = false>
 __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t *st, int x0, int y, int z, int w,
-                                              int lane) {
+                                              int lane, const uint32_t (*sm)[2] = nullptr,
+                                              const uint32_t (*wm)[2] = nullptr, const uint32_t (*bnc)[Q] = nullptr,
+                                              float *fxw = nullptr, float *fzw = nullptr, int *hit = nullptr) {
   using PK = Pack16<DT>;
   const Geom &g = p.g;
   const bool live = INTERIOR || x0 < g.nx;
   const bool has_b = INTERIOR || x0 + 1 < g.nx;
   const bool has_r = INTERIOR || x0 + 2 < g.nx;
   const bool inlet = !INTERIOR && x0 == 0;
-  const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
+  const int c0 = (z * g.ny + y) * g.pitch + x0;
+  const int c = live ? chk(p, c0) : c0;                             // a lane past the row end uses no offset
   const int lane_word = 4 + lane;                                     // 32-bit word of elements 8 + 2 lane, + 1
   f2 v[Q];
   static_for<0, Q>([&](auto I) {
@@ -171,119 +176,18 @@ __device__ __forceinline__ void tma_pair_fast(const StepParams &p, const uint8_t
       const float2 o = PK::both(own);
       v[i] = F2(has_b ? o.y : o.x, has_r ? PK::lo(right) : o.y);
     }
+    if constexpr (CHECKED && i > 0) pair_link<DT, i>(v[i], *sm, *wm, (*bnc)[i], *fxw, *fzw, *hit);
   });
   if (!live) return;
   // accumulating steps: the pair's old sums from the staged box [4 sums][4 rows][64 cells], read where added
   const double2 *acc_box = reinterpret_cast<const double2 *>(st + kTmaStageBytes) + w * 32 + lane;
-  pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_box[k * 4 * 32]; });
-}
-
-// The link masks of one cell of the checked path, for the flags of its pull
-// sources as step_cell maps them (lbm3d.py:77-95): bit i of `solid` is set when
-// link i's source is not fluid, bit i of `wall` when it is a stone; bit 0 of
-// `solid` marks a cell that is itself not fluid (or lies past the row end).
-// The inlet column pulls nothing.  Every load is issued before any is used.
-template <typename Ctx>
-__device__ __forceinline__ void cell_links(const Ctx &p, int x, int y, int z, uint32_t &solid, uint32_t &wall) {
-  const Geom &g = p.g;
-  solid = 1u;
-  wall = 0u;
-  if (x >= g.nx) return;
-  const int c = chk(p, (z * g.ny + y) * g.pitch + x);
-  const uint8_t own = p.flag[c];
-  if (x > 0) {
-    const int row = g.pitch, lev = g.ny * g.pitch;
-    const int off_xm = c - 1;
-    const int off_xp = (x + 1 >= g.nx) ? c : c + 1;
-    const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
-    const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
-    const int off_zm = -lev;
-    const int off_zp = (z == g.nz - 1) ? 0 : lev;
-    uint8_t fs[Q];
-    static_for<1, Q>([&](auto I) {
-      constexpr int i = decltype(I)::value;
-      constexpr int ex = CX(i), ey = CY(i), ez = CZ(i);
-      if (ez == 1 && z == 0) {
-        fs[i] = (uint8_t)SW_GROUND;
-      } else {
-        const int src = chk(p, (ex == 1 ? off_xm : ex == -1 ? off_xp : c) + (ey == 1 ? off_ym : ey == -1 ? off_yp : 0) +
-                                   (ez == 1 ? off_zm : ez == -1 ? off_zp : 0));
-        fs[i] = __ldg(p.flag + src);
-      }
-    });
-    uint32_t sm = 0u, wm = 0u;
-    static_for<1, Q>([&](auto I) {
-      constexpr int i = decltype(I)::value;
-      sm |= (fs[i] != 0 ? 1u : 0u) << i;
-      wm |= (fs[i] == SW_WALL ? 1u : 0u) << i;
-    });
-    solid = sm;
-    wall = wm;
+  if constexpr (CHECKED) {
+    const uint32_t keep = pair_solid_cells(v, *sm);
+    if (keep == 0u) return;
+    pair_collide_store<DT, ACC, true>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_box[k * 4 * 32]; }, keep);
   } else {
-    solid = 0u;
+    pair_collide_store<DT, ACC>(p, v, x0, c, z, inlet, has_b, [&](int k) { return acc_box[k * 4 * 32]; });
   }
-  if (own != 0) {
-    solid = 1u;
-    wall = 0u;
-  }
-}
-
-// The checked path's inputs: pulled values from the staged boxes (the box of
-// the link's population holds its source row, the z mirror at the top, the
-// periodic wrap rows beside the stage, x from x0s - 8; the outlet copies
-// column x), flags as the link masks of cell_links and bounce-back values from
-// `bnc`: the 32-bit pair (cells x0, x0 + 1) of population OPP(i) at the pair's
-// own offset, loaded for the links that bounce in either cell; `half` picks
-// this cell's 16 bits.
-template <int DT> struct TmaPull {
-  using T = typename Store<DT>::T;
-  const uint8_t *st;
-  int xl;        // x - x0s
-  int x, y, w;
-  const Geom &g;
-  uint32_t solid, wall;
-  const uint32_t (&bnc)[Q];
-  int half;
-  template <int I, int P, typename Ctx>
-  __device__ __forceinline__ float operator()(Int<I>, Int<P>, const Ctx &, int) const {
-    constexpr int ex = CX(I), ey = CY(I);
-    const uint8_t *rowp = st + I * kTmaBoxBytes + w * kTmaRowBytes;
-    if constexpr (ey == 1) {
-      if (y == 0) rowp = st + Q * kTmaBoxBytes + wrap_slot(I) * kTmaWrapBytes;
-    } else if constexpr (ey == -1) {
-      if (y == g.ny - 1) rowp = st + Q * kTmaBoxBytes + wrap_slot(I) * kTmaWrapBytes;
-    }
-    const int e = (ex == -1 && x + 1 >= g.nx) ? xl + 8 : xl + 8 - ex;
-    return Store<DT>::to_shifted(reinterpret_cast<const T *>(rowp)[e]);
-  }
-  template <typename Ctx> __device__ __forceinline__ bool self_solid(const Ctx &, int) const { return solid & 1u; }
-  template <int I, typename Ctx> __device__ __forceinline__ uint8_t src_flag(Int<I>, const Ctx &, int, int) const {
-    return ((solid >> I) & 1u) ? (((wall >> I) & 1u) ? (uint8_t)SW_WALL : (uint8_t)SW_GROUND) : (uint8_t)0;
-  }
-  template <int I, typename Ctx> __device__ __forceinline__ float bounce(Int<I>, const Ctx &, int) const {
-    return half ? Pack16<DT>::hi(bnc[I]) : Pack16<DT>::lo(bnc[I]);
-  }
-};
-
-// Before the wait of a checked item: the link masks of the lane's two cells
-// and the bounce-back pairs of the links that bounce in either cell.  The input
-// lattice is not written during the step, so these loads may run ahead of the
-// staged copies and their latency overlaps the copies'.
-template <int DT, typename Ctx>
-__device__ __forceinline__ void tma_checked_prefetch(const Ctx &p, int x0, int y, int z, uint32_t (&sm)[2],
-                                                     uint32_t (&wm)[2], uint32_t (&bnc)[Q]) {
-  using T = typename Store<DT>::T;
-  const Geom &g = p.g;
-  cell_links(p, x0, y, z, sm[0], wm[0]);
-  cell_links(p, x0 + 1, y, z, sm[1], wm[1]);
-  const uint32_t any = (sm[0] | sm[1]) & ~1u;                 // no link bit in a lane past the row end
-  const int c = (z * g.ny + y) * g.pitch + x0;                // even: the pair is one aligned 32-bit word
-  static_for<1, Q>([&](auto I) {
-    constexpr int i = decltype(I)::value;
-    bnc[i] = ((any >> i) & 1u) ? __ldg(reinterpret_cast<const unsigned int *>(p.template in<T>(OPP(i)) + chk(p, c)))
-                               : 0u;
-  });
-  bnc[0] = 0u;
 }
 
 // Grid: (ceil(pitch / 64), ceil(ceil(ny / 4) / ITEMS), nz); block = 4 warps, warp w = row y0 + w.
@@ -340,7 +244,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
     const bool work = y < g.ny && !(ka & kb & TILE_ALL_SOLID);
     const bool checked = work && ((ka | kb) & TILE_CHECK);          // uniform across the warp
     uint32_t sm[2], wm[2], bnc[Q];
-    if (checked) tma_checked_prefetch<DT>(p, x0, y, z, sm, wm, bnc);
+    if (checked) pair_links_prefetch<DT>(p, x0, y, z, sm, wm, bnc);
     if (ok) ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((j / Cfg::NSTAGE) & 1), polls);
     if (ok && work) {
       if (!checked) {
@@ -348,16 +252,10 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
           tma_pair_fast<DT, ACC, true>(p, smem + s * kStage, x0, y, z, w, lane);
         else
           tma_pair_fast<DT, ACC, false>(p, smem + s * kStage, x0, y, z, w, lane);
-      } else {                                                        // next to stones / ground: per cell
-        float fxw = 0.0f, fzw = 0.0f;                                 // (sources from the staged boxes)
+      } else {                                                        // next to stones / the ground
+        float fxw = 0.0f, fzw = 0.0f;
         int hit = 0;
-        const uint8_t *stp = smem + s * kStage;
-        if (x0 < g.nx)
-          step_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit,
-                                   TmaPull<DT>{stp, 2 * lane, x0, y, w, g, sm[0], wm[0], bnc, 0});
-        if (x0 + 1 < g.nx)
-          step_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit,
-                                   TmaPull<DT>{stp, 2 * lane + 1, x0 + 1, y, w, g, sm[1], wm[1], bnc, 1});
+        tma_pair_fast<DT, ACC, false, true>(p, smem + s * kStage, x0, y, z, w, lane, &sm, &wm, &bnc, &fxw, &fzw, &hit);
         if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
       }
     }
