@@ -302,6 +302,21 @@ int sw_coefficients(const int64_t *force, int64_t n_steps, int32_t nz, double UH
  * left).  A solve's statistics then need 48 bytes downloaded, not its force series. */
 int sw_coef_stats(const double *coef, int64_t n_steps, int64_t n_spin, double *stats, sw_stream s);
 
+/* Recirculation area behind the wall (export3d.py:169-184; replaces the host
+ * computation on the every-2nd-cell mean field of lbm3d.py:412).  On the cells
+ * (2 i, 2 j, 2 k) with X0/2 <= i < min(ceil(nx/2), (X0 + 10 H)/2), every j,
+ * k < min(ceil(nz/2), H): u_x of the time mean acc[1] / max(n_acc, 1) (acc: the
+ * float64 sums [4][nz][ny][pitch] of sw_macro_accum / sw_step), 0.05 at
+ * non-fluid cells, over U_H; level k = 0 copies level 1; one separable 3-point
+ * box blur with edge clamping; *count (device int64) = the cells below zero.
+ * The area in H^2 per unit wall length is count * 8 / (H^2 ny).  scratch:
+ * sw_recirc_scratch_bytes() bytes of device memory (4-byte aligned);
+ * sw_recirc_scratch_bytes returns SW_ERR_BAD_ARG when the box is empty or has
+ * fewer than two levels. */
+int64_t sw_recirc_scratch_bytes(const sw_geom *g, int32_t H, int32_t X0);
+int sw_recirc_count(const sw_geom *g, const double *acc, int64_t n_acc, const uint8_t *flag, int32_t H, int32_t X0,
+                    double UH, void *scratch, int64_t scratch_bytes, int64_t *count, sw_stream s);
+
 /* ---------------------------------------------------------------- wall masks on the device
  * The per-cell work of the two stone-wall generators of the Python package
  * (stonewall/geometry.py); their random draws stay on the host, so a seed gives

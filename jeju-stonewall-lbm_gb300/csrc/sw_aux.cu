@@ -425,6 +425,67 @@ cudaError_t aux_coef_stats(const double *coef, long long n_steps, long long n_sp
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- recirculation area
+// export3d.py:169-184 on the every-2nd-cell mean field (lbm3d.py:412): the box
+// of cells (2 (i0 + i), 2 j, 2 k), i < I, j < J, k < K, holds u_x of the time
+// mean (sums / n_acc in float64, rounded to float) or 0.05 at non-fluid cells,
+// divided by U_H in float; level k = 0 takes level 1's value; one 3-point box
+// blur with edge clamping along i, then j, then k ((a + b) + c, then / 3, in
+// float); the reverse-flow cells are those left below zero.  Built without FMA
+// contraction (the file's --fmad=false) and with explicitly rounded operations,
+// so the count equals the float32 NumPy restatement's.  Scratch layout
+// [k][j][i].
+struct RecircBox {
+  int i0, I, J, K;
+};
+__global__ void k_recirc_gather(Geom g, RecircBox b, const double *acc, double n, const uint8_t *flag, float uh,
+                                float *out) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)b.I * b.J * b.K) return;
+  const int i = (int)(e % b.I), j = (int)((e / b.I) % b.J), k = (int)(e / ((long long)b.I * b.J));
+  const int x = 2 * (b.i0 + i), y = 2 * j, z = 2 * (k == 0 ? 1 : k);
+  const size_t c = ((size_t)z * g.ny + y) * g.pitch + x;
+  const float v = flag[c] != 0 ? 0.05f : __double2float_rn(__ddiv_rn(acc[(size_t)g.plane + c], n));
+  out[e] = __fdiv_rn(v, uh);
+}
+// AXIS 0: i, 1: j, 2: k.  With COUNT the result is not stored: each cell below
+// zero adds one to *count (one atomic per warp).
+template <int AXIS, bool COUNT>
+__global__ void k_recirc_blur(RecircBox b, const float *in, float *out, unsigned long long *count) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)b.I * b.J * b.K;
+  bool neg = false;
+  if (e < n) {
+    const int i = (int)(e % b.I), j = (int)((e / b.I) % b.J), k = (int)(e / ((long long)b.I * b.J));
+    const int at = AXIS == 0 ? i : AXIS == 1 ? j : k;
+    const int len = AXIS == 0 ? b.I : AXIS == 1 ? b.J : b.K;
+    const long long step = AXIS == 0 ? 1 : AXIS == 1 ? (long long)b.I : (long long)b.I * b.J;
+    const float lo = in[e - (at > 0 ? step : 0)], mid = in[e], hi = in[e + (at + 1 < len ? step : 0)];
+    const float v = __fdiv_rn(__fadd_rn(__fadd_rn(lo, mid), hi), 3.0f);
+    if (COUNT) neg = v < 0.0f;
+    else out[e] = v;
+  }
+  if (COUNT) {
+    const unsigned m = __ballot_sync(0xffffffffu, neg);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+  }
+}
+cudaError_t aux_recirc_count(const Geom &g, int i0, int I, int J, int K, const double *acc, long long n_acc,
+                             const uint8_t *flag, float uh, float *scratch, long long *count, cudaStream_t s) {
+  const RecircBox b{i0, I, J, K};
+  const long long n = (long long)I * J * K;
+  float *a = scratch, *t = scratch + n;
+  unsigned long long *cnt = reinterpret_cast<unsigned long long *>(count);
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(*cnt), s);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  k_recirc_gather<<<blocks, 256, 0, s>>>(g, b, acc, (double)(n_acc > 0 ? n_acc : 1), flag, uh, a);
+  k_recirc_blur<0, false><<<blocks, 256, 0, s>>>(b, a, t, nullptr);
+  k_recirc_blur<1, false><<<blocks, 256, 0, s>>>(b, t, a, nullptr);
+  k_recirc_blur<2, true><<<blocks, 256, 0, s>>>(b, a, nullptr, cnt);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- viewer payload
 // k_slice_xz / k_slice_xy (lbm3d.py:191-200): the macro field u (device layout
 // [4][nz][ny][pitch]) at y = y0 or z = z0, written in the reference layout

@@ -21,6 +21,8 @@ cudaError_t aux_force_to_f64(const long long *fx, double *out, long long n, cuda
 cudaError_t aux_coefficients(const long long *force, long long n_steps, int nz, double qa, double H, double *coef,
                              cudaStream_t s);
 cudaError_t aux_coef_stats(const double *coef, long long n_steps, long long n_spin, double *stats, cudaStream_t s);
+cudaError_t aux_recirc_count(const Geom &g, int i0, int I, int J, int K, const double *acc, long long n_acc,
+                             const uint8_t *flag, float uh, float *scratch, long long *count, cudaStream_t s);
 cudaError_t aux_slice_xz(const Geom &g, const float *u, int y0, float *out, cudaStream_t s);
 cudaError_t aux_slice_xy(const Geom &g, const float *u, int z0, float *out, cudaStream_t s);
 cudaError_t aux_qcoarse(const Geom &g, const float *u, const uint8_t *flag, int x0, int ds, int di, int dj, int dk,

@@ -2,6 +2,7 @@
 //
 // Every entry point validates its arguments, launches on the caller's stream
 // and returns an SW_* status; nothing here allocates or synchronises.
+#include <algorithm>
 #include <cstdio>
 
 #include "sw_aa.cuh"
@@ -395,6 +396,40 @@ int sw_coef_stats(const double *coef, int64_t n_steps, int64_t n_spin, double *s
   if (n_steps < 0 || n_spin < 0 || !stats || (n_steps > 0 && !coef)) return SW_ERR_BAD_ARG;
   clear_stale();
   return cuda_status(sw::aux_coef_stats(coef, n_steps, n_spin, stats, st(s)));
+}
+
+// The box of the recirculation count (export3d.py:177-179 on the every-2nd-cell
+// field): i from X0 / 2 to min(ceil(nx / 2), (X0 + 10 H) / 2), every j, k below
+// min(ceil(nz / 2), H); false when it is empty or has fewer than two levels.
+static bool recirc_box(const sw_geom *g, int32_t H, int32_t X0, int &i0, int &I, int &J, int &K) {
+  if (!geom_ok(g) || H <= 0 || X0 < 0) return false;
+  const long long nxd = (g->nx + 1) / 2, nzd = (g->nz + 1) / 2;
+  const long long i1 = std::min(nxd, ((long long)X0 + 10ll * H) / 2);
+  i0 = X0 / 2;
+  I = (int)(i1 - i0);
+  J = (g->ny + 1) / 2;
+  K = (int)std::min(nzd, (long long)(2ll * H) / 2);
+  return I > 0 && J > 0 && K >= 2;
+}
+
+int64_t sw_recirc_scratch_bytes(const sw_geom *g, int32_t H, int32_t X0) {
+  int i0, I, J, K;
+  if (!recirc_box(g, H, X0, i0, I, J, K)) return SW_ERR_BAD_ARG;
+  return 2ll * I * J * K * (int64_t)sizeof(float);
+}
+
+int sw_recirc_count(const sw_geom *g, const double *acc, int64_t n_acc, const uint8_t *flag, int32_t H, int32_t X0,
+                    double UH, void *scratch, int64_t scratch_bytes, int64_t *count, sw_stream s) {
+  int i0, I, J, K;
+  if (!recirc_box(g, H, X0, i0, I, J, K) || !acc || !flag || !scratch || !count || n_acc < 0 || !(UH > 0.0))
+    return SW_ERR_BAD_ARG;
+  if (scratch_bytes < 2ll * I * J * K * (int64_t)sizeof(float) || (reinterpret_cast<uintptr_t>(scratch) & 3u) ||
+      (reinterpret_cast<uintptr_t>(count) & 7u))
+    return SW_ERR_BAD_ARG;
+  clear_stale();
+  return cuda_status(sw::aux_recirc_count(to_geom(g), i0, I, J, K, acc, n_acc, flag, (float)UH,
+                                          static_cast<float *>(scratch), reinterpret_cast<long long *>(count),
+                                          st(s)));
 }
 
 int sw_slice_xz(const sw_geom *g, const float *u, int32_t y0, float *out, sw_stream s) {

@@ -117,6 +117,8 @@ def load(path):
         "sw_force_to_f64": ([P, P, i64, P], ctypes.c_int),
         "sw_coefficients": ([P, i64, i32, f64, f64, i32, P, P], ctypes.c_int),
         "sw_coef_stats": ([P, i64, i64, P, P], ctypes.c_int),
+        "sw_recirc_scratch_bytes": ([G, i32, i32], i64),
+        "sw_recirc_count": ([G, P, i64, P, i32, i32, f64, P, i64, P, P], ctypes.c_int),
         "sw_pack_box_bytes": ([i32, i32, i32], i64),
         "sw_pack_ellipsoids": ([P, i32, i32, i32, i32, i32, f64, P, P, P], ctypes.c_int),
         "sw_voxelize_stones": ([P, i32, i32, i32, i32, P, P, i32, P], ctypes.c_int),

@@ -12,6 +12,9 @@ device_stats():  the same two steps on the GPU from the device force series
 recirculation_area(): export3d.py:169-184 -- cells of the every-2nd-cell mean
                  field with u_x < 0 in [X0, X0 + 10H) x [0, 2H) after the
                  same masking and one 3-point box blur, times 8 / (H^2 ny).
+device_recirculation_area(): the same from the device float64 sums
+                 (sw_recirc_count): the box, blur and count on the GPU, 8 bytes
+                 back instead of the mean field.
 """
 import numpy as np
 
@@ -63,6 +66,26 @@ def device_stats(force, UH, H, ny, n_spin, stream=None):
     N.check(N.lib().sw_coef_stats(_ptr(coef), force.n_steps, int(n_spin), _ptr(out), _stream(stream)),
             "sw_coef_stats")
     return dict(zip(STAT_KEYS, (float(v) for v in out.cpu().tolist())))
+
+
+def device_recirculation_area(accum, n_acc, flags, H, X0, UH, stream=None):
+    """recirculation_area() of the time-mean field on the GPU, from the float64 sums in a
+    stonewall.fields.Accum (n_acc accumulated states) and the Flags of the same grid: the
+    every-2nd-cell box, blur and count run on the device and 8 bytes come back.  Equal to
+    recirculation_area(mean_ux[::2, ::2, ::2], (flag != 0)[::2, ::2, ::2], H, X0, UH, ny)."""
+    import torch
+    from . import _native as N
+    from .fields import _ptr, _stream
+    g = accum.grid
+    L = N.lib()
+    nbytes = L.sw_recirc_scratch_bytes(g.gp, int(H), int(X0))
+    if nbytes < 0:
+        raise ValueError(f"no recirculation box for H={H}, X0={X0} on {g.nx}x{g.ny}x{g.nz}")
+    scratch = torch.empty(nbytes // 4, dtype=torch.float32, device=accum.data.device)
+    count = torch.empty(1, dtype=torch.int64, device=accum.data.device)
+    N.check(L.sw_recirc_count(g.gp, accum.ptr, int(n_acc), flags.ptr, int(H), int(X0), float(UH), _ptr(scratch),
+                              nbytes, _ptr(count), _stream(stream)), "sw_recirc_count")
+    return float(int(count.item()) * 8) / (H ** 2 * g.ny)
 
 
 def fx_profile(force, UH, ny, n_spin):

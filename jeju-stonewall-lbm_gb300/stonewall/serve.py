@@ -43,7 +43,7 @@ import torch
 
 from .batch import Batch
 from .geometry import ellipsoid_wall
-from .metrics import coefficients, device_stats, stats
+from .metrics import coefficients, device_recirculation_area, device_stats, recirculation_area, stats
 from .params import baseline_params, flags_from_wall
 from . import trace
 from .solver import DeviceWaitTimeout, Diverged, WallSolver
@@ -117,16 +117,22 @@ def failure_result(req, s, err, now):
 
 
 def solve_stats(s):
-    """The solve's Cd / Cm statistics, reduced on the GPU (48 bytes read back instead of the force series)."""
+    """The solve's Cd / Cm statistics and recirculation area, reduced on the GPU (56 bytes read back
+    instead of the force series and the mean field)."""
     p = s.params
-    return device_stats(s.force, p.UH, p.H, p.ny, s.n_spin)
+    st = device_stats(s.force, p.UH, p.H, p.ny, s.n_spin)
+    st["recirc"] = device_recirculation_area(s.acc, s.n_acc, s.flags, p.H, p.X0, p.UH)
+    return st
 
 
 def solve_stats_host(s):
-    """The same statistics from the downloaded force series (stonewall.metrics on the host)."""
+    """The same statistics from the downloaded force series and mean field (stonewall.metrics on the host)."""
     p = s.params
     co = coefficients(s.force_series(), p.UH, p.H, p.ny)
-    return stats(co["Cd"], co["Cm"], co["Cl"], s.n_spin)
+    st = stats(co["Cd"], co["Cm"], co["Cl"], s.n_spin)
+    wall = s.flags.numpy() != 0
+    st["recirc"] = recirculation_area(s.mean_field()[1][::2, ::2, ::2], wall[::2, ::2, ::2], p.H, p.X0, p.UH, p.ny)
+    return st
 
 
 class Server:

@@ -29,7 +29,7 @@ import numpy as np
 import torch
 
 from .geometry import ellipsoid_wall
-from .metrics import coefficients, recirculation_area, stats
+from .metrics import coefficients, device_recirculation_area, stats
 from .params import baseline_params, flags_from_wall
 from .solver import WallSolver
 
@@ -49,9 +49,7 @@ def solve(p, flag, dtype, seed, steps, noise_seed=None):
     ms = e0.elapsed_time(e1)
     co = coefficients(s.force_series(), p.UH, p.H, p.ny)
     st = stats(co["Cd"], co["Cm"], co["Cl"], p.n_spin)
-    mean_ux = s.mean_field()[1]
-    wall = flag != 0
-    st["recirc"] = recirculation_area(mean_ux[::2, ::2, ::2], wall[::2, ::2, ::2], p.H, p.X0, p.UH, p.ny)
+    st["recirc"] = device_recirculation_area(s.acc, s.n_acc, s.flags, p.H, p.X0, p.UH)
     st["mlups"] = s.grid.cells * steps / (ms * 1e-3) / 1e6
     st["seconds"] = ms * 1e-3
     del s

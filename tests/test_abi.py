@@ -79,6 +79,18 @@ def test_entry_points_reject_bad_arguments_before_launching(native_lib):
                              None) == N.SW_ERR_BAD_ARG                                             # misaligned rows
     assert L.sw_coef_stats(p, 4, -1, p, None) == N.SW_ERR_BAD_ARG
     assert L.sw_coef_stats(p, 4, 0, None, None) == N.SW_ERR_BAD_ARG
+    # recirculation box on 32x4x4, H = 2, X0 = 4: i in [2, 12), j < 2, k < 2 -> two float buffers
+    assert L.sw_recirc_scratch_bytes(gp, 2, 4) == 2 * 10 * 2 * 2 * 4
+    assert L.sw_recirc_scratch_bytes(gp, 1, 4) == N.SW_ERR_BAD_ARG                              # one level
+    assert L.sw_recirc_scratch_bytes(gp, 2, 40) == N.SW_ERR_BAD_ARG                             # past the outlet
+    assert L.sw_recirc_scratch_bytes(gp, 0, 4) == N.SW_ERR_BAD_ARG
+    p8 = ctypes.c_void_p(buf.ctypes.data + 8)
+    assert L.sw_recirc_count(gp, p, 1, p, 2, 4, 0.05, p, 100, p8, None) == N.SW_ERR_BAD_ARG      # scratch small
+    assert L.sw_recirc_count(gp, p, 1, p, 2, 4, 0.0, p, 320, p8, None) == N.SW_ERR_BAD_ARG       # U_H
+    assert L.sw_recirc_count(gp, p, -1, p, 2, 4, 0.05, p, 320, p8, None) == N.SW_ERR_BAD_ARG     # n_acc
+    assert L.sw_recirc_count(gp, p, 1, p, 2, 4, 0.05, p, 320, ctypes.c_void_p(buf.ctypes.data + 4),
+                             None) == N.SW_ERR_BAD_ARG                                           # count misaligned
+    assert L.sw_recirc_count(gp, None, 1, p, 2, 4, 0.05, p, 320, p8, None) == N.SW_ERR_BAD_ARG
 
 
 def test_status_words_map_to_errors(native_lib):
