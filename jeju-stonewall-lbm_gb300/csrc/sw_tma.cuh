@@ -17,9 +17,11 @@
 // Boxes start on 16-byte boundaries (x0 - 8 is a multiple of 8 halves); a box
 // reaching outside the lattice reads zeros there: x < 0 only feeds the inlet
 // cell (which does not pull), x >= nx only the outlet copy (handled by the
-// same per-lane selects as k_step_pair), z < 0 only ground rows (never on the
-// fast path).  The periodic y wrap is not a box: the warp whose source row
-// is -1 or ny reads a one-row box of row ny - 1 or 0 loaded beside the stage.
+// same per-lane selects as k_step_pair), z < 0 only links from the ground
+// below the bottom level (segments there take the checked path, which puts the
+// bounce-back values in their place).  The periodic y wrap is not a box: the
+// warp whose source row is -1 or ny reads a one-row box of row ny - 1 or 0
+// loaded beside the stage.
 //
 // A block runs ITEMS consecutive y row-groups of one 64-cell x segment pair at
 // one level, with NSTAGE stages in flight.  When ITEMS > NSTAGE the stages form a
