@@ -223,3 +223,12 @@ def test_16bit_accumulating_step_sums_match_oracle(dtype, cfg, cuda, oracle_mod)
         got = acc.numpy(solid=flag != 0, n_acc=1)
         np.testing.assert_allclose(got[0], u[0], rtol=2e-6, atol=0)
         np.testing.assert_allclose(got[1:], u[1:], rtol=0, atol=2e-6 * np.abs(u[1:]).max())
+
+
+def test_bf16_storage_warns(cuda):
+    """bf16 shifted storage stays available (it is measured in the precision study) but says what it costs."""
+    from gpu_helpers import inlet, make_mask
+    from stonewall.solver import BiasedStorageWarning, WallSolver
+    flag = make_mask(45, 7, 10, 1)
+    with pytest.warns(BiasedStorageWarning, match="bf16"):
+        WallSolver(flag, inlet(10, 3), 2e-3, 0.1, 36, 10, dtype="bf16")
