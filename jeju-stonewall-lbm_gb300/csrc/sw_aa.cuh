@@ -323,6 +323,44 @@ __device__ __forceinline__ void aa_pair_even_fast(const StepParams &p, int x0, i
   pair_collide_store<DT, ACC>(p, v, x0, c, z, x0 == 0, has_b, [&](int k) { return acc_old[k]; });
 }
 
+// The collision and scatter of an interior odd-step cell pair (see
+// aa_pair_odd_interior), with the old float64 sums of the pair in acc_old.
+template <int DT, bool ACC>
+__device__ __forceinline__ void aa_pair_collide_scatter(const StepParams &p, const f2 (&v)[Q], int x0, int c,
+                                                        int off_ym, int off_yp, int lev, int lane,
+                                                        const double2 (&acc_old)[4]) {
+  using S = Store<DT>;
+  using T = typename S::T;
+  using PK = Pack16<DT>;
+  const Phys<float> ph = phys<float>(p);
+  f2 rho, ux, uy, uz;
+  collide2(v, x0, true, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz, p.status,
+           [&](auto I, f2 o) {
+             constexpr int k = decltype(I)::value;
+             constexpr int ex = CX(k), ey = CY(k), ez = CZ(k);
+             T *plane = p.template out<T>(k);
+             const int t = c + (ey == 1 ? off_yp : ey == -1 ? off_ym : 0) + ez * lev;   // target row, column x0
+             if constexpr (ex == 0) {
+               *reinterpret_cast<uint32_t *>(plane + chk(p, t)) = PK::pack(o.v.x, o.v.y);
+             } else {
+               // targets x0 + ex (first cell) and x0 + 1 + ex (second cell); lane L writes the
+               // word holding its second target and lane L + 1's first
+               const float nxt = __shfl_down_sync(0xffffffffu, o.v.x, 1);
+               const int w = chk(p, t + (ex == 1 ? 2 : 0));
+               if (lane < 31) *reinterpret_cast<uint32_t *>(plane + w) = PK::pack(o.v.y, nxt);
+               else plane[w] = S::from_shifted(o.v.y);                 // the other half is the next warp's
+               if (lane == 0) plane[chk(p, t + (ex == 1 ? 1 : -1))] = S::from_shifted(o.v.x);   // the previous warp's
+             }
+           });
+  if (ACC) {
+    const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
+    *reinterpret_cast<double2 *>(p.accp(0) + c) = make_double2(v0.x + (double)rho.v.x, v0.y + (double)rho.v.y);
+    *reinterpret_cast<double2 *>(p.accp(1) + c) = make_double2(v1.x + (double)ux.v.x, v1.y + (double)ux.v.y);
+    *reinterpret_cast<double2 *>(p.accp(2) + c) = make_double2(v2.x + (double)uy.v.x, v2.y + (double)uy.v.y);
+    *reinterpret_cast<double2 *>(p.accp(3) + c) = make_double2(v3.x + (double)uz.v.x, v3.y + (double)uz.v.y);
+  }
+}
+
 // Odd step, fast path of an interior segment pair (not the inlet or the outlet
 // segment pair, not the top level; every pull source and scatter target is a
 // fluid cell inside the lattice): pull as the two-lattice pair kernel does, then
@@ -371,33 +409,7 @@ __device__ __forceinline__ void aa_pair_odd_interior(const StepParams &p, int x0
       v[i] = F2(own.y, lane == 31 ? edge[i] : PK::lo(next));
     }
   });
-  const Phys<float> ph = phys<float>(p);
-  f2 rho, ux, uy, uz;
-  collide2(v, x0, true, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz, p.status,
-           [&](auto I, f2 o) {
-             constexpr int k = decltype(I)::value;
-             constexpr int ex = CX(k), ey = CY(k), ez = CZ(k);
-             T *plane = p.template out<T>(k);
-             const int t = c + (ey == 1 ? off_yp : ey == -1 ? off_ym : 0) + ez * lev;   // target row, column x0
-             if constexpr (ex == 0) {
-               *reinterpret_cast<uint32_t *>(plane + chk(p, t)) = PK::pack(o.v.x, o.v.y);
-             } else {
-               // targets x0 + ex (first cell) and x0 + 1 + ex (second cell); lane L writes the
-               // word holding its second target and lane L + 1's first
-               const float nxt = __shfl_down_sync(0xffffffffu, o.v.x, 1);
-               const int w = chk(p, t + (ex == 1 ? 2 : 0));
-               if (lane < 31) *reinterpret_cast<uint32_t *>(plane + w) = PK::pack(o.v.y, nxt);
-               else plane[w] = S::from_shifted(o.v.y);                 // the other half is the next warp's
-               if (lane == 0) plane[chk(p, t + (ex == 1 ? 1 : -1))] = S::from_shifted(o.v.x);   // the previous warp's
-             }
-           });
-  if (ACC) {
-    const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
-    *reinterpret_cast<double2 *>(p.accp(0) + c) = make_double2(v0.x + (double)rho.v.x, v0.y + (double)rho.v.y);
-    *reinterpret_cast<double2 *>(p.accp(1) + c) = make_double2(v1.x + (double)ux.v.x, v1.y + (double)ux.v.y);
-    *reinterpret_cast<double2 *>(p.accp(2) + c) = make_double2(v2.x + (double)uy.v.x, v2.y + (double)uy.v.y);
-    *reinterpret_cast<double2 *>(p.accp(3) + c) = make_double2(v3.x + (double)uz.v.x, v3.y + (double)uz.v.y);
-  }
+  aa_pair_collide_scatter<DT, ACC>(p, v, x0, c, off_ym, off_yp, lev, lane, acc_old);
 }
 
 // Grid: (ceil(pitch / 64), ceil(ny / WY), nz); warp = two adjacent row segments.
@@ -441,6 +453,154 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
   if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
 }
 
+// ---------------------------------------------------------------- TMA-staged 16-bit AA steps
+// The AA steps with their sources staged in shared memory by TMA, as k_step_tma
+// does for the two-lattice step (one item of 4 rows x 64 cells per block, all
+// copies issued at the start, bounded waits).  Odd step: the boxes are the
+// two-lattice step's (natural planes at the source rows and levels); an
+// interior warp (not the inlet or outlet segment pair, not the top level, not
+// next to stones or the ground) pulls from them and scatters as
+// aa_pair_odd_interior does; the other warps run the per-cell odd step.  Even
+// step: box i is plane opp(i) -- slot i -- at the item's own rows and level;
+// every warp not next to stones or the ground collides from it as
+// aa_pair_even_fast does.  In place and race-free: every value a cell uses
+// from a box is written in this step only by that cell, after its wait; the
+// rest of a box (columns and rows of neighbouring items) may be read while
+// its owners rewrite it, and is not used.
+
+// Even step: the 19 own-slot boxes of item (x0, y0, z) and with ACC its sums.
+template <bool ACC>
+__device__ __forceinline__ void tma_issue_own(const CUtensorMap *map, const CUtensorMap *map_acc, int x0, int y0, int z,
+                                              uint32_t st, uint32_t bar) {
+  mbar_expect_tx(bar, Q * kTmaBoxBytes + (ACC ? kTmaAccBytes : 0));
+  static_for<0, Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    tma_load_4d(st + i * kTmaBoxBytes, map, x0 - 8, y0, z, OPP(i), bar);
+  });
+  if constexpr (ACC) tma_load_4d(st + kTmaStageBytes, map_acc, x0, y0, z, 0, bar);
+}
+
+template <int DT, bool ODD, bool ACC>
+__global__ void __launch_bounds__(128, 9)
+    k_step_aa_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap map1,
+                  const __grid_constant__ CUtensorMap map_acc, const __grid_constant__ StepParams p, AAParams a) {
+  using PK = Pack16<DT>;
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  __shared__ __align__(8) unsigned long long bar;
+  uint8_t *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  const Geom &g = p.g;
+  const int w = threadIdx.y, lane = threadIdx.x;
+  const bool leader = w == 0 && lane == 0;
+  const int bx = blockIdx.x, z = blockIdx.z;
+  const int x0s = 2 * SEG * bx, y0 = blockIdx.y * 4, y = y0 + w, x0 = x0s + 2 * lane;
+  const uint32_t st = smem_u32(smem);
+  if (leader) {
+    mbar_init(smem_u32(&bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (ODD) tma_issue<ACC>(&map, &map1, &map_acc, g, x0s, y0, z, st, smem_u32(&bar));
+    else tma_issue_own<ACC>(&map, &map_acc, x0s, y0, z, st, smem_u32(&bar));
+  }
+  const int sa = 2 * bx;
+  uint8_t ka = TILE_ALL_SOLID, kb = TILE_ALL_SOLID;
+  if (y < g.ny) {
+    const int seg = (z * g.ny + y) * g.nseg_x + sa;
+    ka = __ldg(p.tiles + seg);
+    kb = sa + 1 < g.nseg_x ? __ldg(p.tiles + seg + 1) : (uint8_t)TILE_ALL_SOLID;
+  }
+  __syncthreads();
+  bool ok = mbar_wait(smem_u32(&bar), 0u, p.tma_poll_limit);
+  if (ok && y < g.ny && !(ka & kb & TILE_ALL_SOLID)) {
+    const int row = g.pitch, lev = g.ny * g.pitch;
+    const int lane_word = 4 + lane;                                   // 32-bit word of elements 8 + 2 lane, + 1
+    if (!((ka | kb) & TILE_CHECK) && !ODD) {                          // even step: own slots, local
+      if (x0 < g.nx) {
+        const bool has_b = x0 + 1 < g.nx;
+        const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
+        f2 v[Q];
+        static_for<0, Q>([&](auto I) {
+          constexpr int i = decltype(I)::value;
+          v[i].v = PK::both(reinterpret_cast<const uint32_t *>(smem + i * kTmaBoxBytes + w * kTmaRowBytes)[lane_word]);
+        });
+        const double2 *acc_box = reinterpret_cast<const double2 *>(smem + kTmaStageBytes) + w * 32 + lane;
+        pair_collide_store<DT, ACC>(p, v, x0, c, z, x0 == 0, has_b, [&](int k) { return acc_box[k * 4 * 32]; });
+      }
+    } else if (!((ka | kb) & TILE_CHECK) && x0s > 0 && x0s + 2 * SEG < g.nx && z < g.nz - 1) {   // odd, interior
+      const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
+      const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
+      const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
+      f2 v[Q];
+      static_for<0, Q>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr int ex = CX(i), ey = CY(i);
+        const uint8_t *rowp = smem + i * kTmaBoxBytes + w * kTmaRowBytes;
+        if constexpr (ey == 1) {
+          if (y == 0) rowp = smem + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes;
+        } else if constexpr (ey == -1) {
+          if (y == g.ny - 1) rowp = smem + Q * kTmaBoxBytes + wrap_slot(i) * kTmaWrapBytes;
+        }
+        const uint32_t *r = reinterpret_cast<const uint32_t *>(rowp);
+        const uint32_t own = r[lane_word];                            // cells x0, x0 + 1
+        if constexpr (ex == 0) {
+          v[i].v = PK::both(own);
+        } else if constexpr (ex == 1) {                               // sources x0 - 1, x0
+          v[i] = F2(PK::hi(r[lane_word - 1]), PK::lo(own));
+        } else {                                                      // sources x0 + 1, x0 + 2
+          v[i] = F2(PK::hi(own), PK::lo(r[lane_word + 1]));
+        }
+      });
+      double2 acc_old[4];
+      if (ACC) {
+        const double2 *acc_box = reinterpret_cast<const double2 *>(smem + kTmaStageBytes) + w * 32 + lane;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc_old[k] = acc_box[k * 4 * 32];
+      }
+      aa_pair_collide_scatter<DT, ACC>(p, v, x0, c, off_ym, off_yp, lev, lane, acc_old);
+    } else {                                                          // per cell (from the lattice)
+      float fxw = 0.0f, fzw = 0.0f;
+      int hit = 0;
+      if ((ka | kb) & TILE_CHECK) {
+        if (ODD) {
+          if (x0 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0, y, z, fxw, fzw, hit);
+          if (x0 + 1 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0 + 1, y, z, fxw, fzw, hit);
+        } else {
+          if (x0 < g.nx) aa_even_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
+          if (x0 + 1 < g.nx) aa_even_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
+        }
+        if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+      } else {                                                        // odd: inlet, outlet, top
+        if (x0 < g.nx) aa_odd_cell<DT, false, ACC>(p, a, x0, y, z, fxw, fzw, hit);
+        if (x0 + 1 < g.nx) aa_odd_cell<DT, false, ACC>(p, a, x0 + 1, y, z, fxw, fzw, hit);
+      }
+    }
+  }
+  ok = __syncthreads_and(ok);
+  if (!ok && leader) {                                                // a wait gave up: let the copies
+    atomicAdd(&g_tma_timeouts, 1u);                                   // in flight land (normal bound)
+    note_status(p, SW_STATUS_TIMEOUT);
+    (void)mbar_wait(smem_u32(&bar), 0u);
+  }
+}
+
+// The TMA-staged AA step on the lattice p.fin (== p.fout); cudaErrorNotSupported
+// when the tensor maps cannot be made (the caller then runs k_step_aa_pair).
+template <int DT, bool ODD, bool ACC>
+cudaError_t launch_aa_tma(const StepParams &p, const AAParams &a, cudaStream_t s) {
+  CUtensorMap map, map1, map_acc;
+  if (!encode_lattice_map(&map, p.fin, p.g, 4) || !encode_lattice_map(&map1, p.fin, p.g, 1))
+    return cudaErrorNotSupported;
+  if (ACC) {
+    if (!encode_acc_map(&map_acc, p.acc, p.g)) return cudaErrorNotSupported;
+  } else {
+    map_acc = map;                                                   // not read
+  }
+  constexpr int smem = tma_stage_bytes<ACC>() + 128;
+  static_assert(smem <= 48 * 1024, "one stage fits the default shared memory of a block");
+  const dim3 grid((unsigned)((p.g.nseg_x + 1) / 2), (unsigned)((p.g.ny + 3) / 4), (unsigned)p.g.nz);
+  k_step_aa_tma<DT, ODD, ACC><<<grid, dim3(32, 4), smem, s>>>(map, map1, map_acc, p, a);
+  return cudaGetLastError();
+}
+
 // One AA step.  odd: reads natural planes, writes slot s to plane opp(s);
 // even: reads slot s from plane opp(s), writes S_k to plane k.
 template <int DT>
@@ -463,7 +623,12 @@ cudaError_t launch_aa(const StepParams &p_in, const AAParams &a, bool odd, cudaS
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  if constexpr (is16(DT)) {                          // two cells per thread
+  if constexpr (is16(DT)) {                          // two cells per thread, sources staged by TMA
+    cudaError_t e = odd ? (p.acc ? launch_aa_tma<DT, true, true>(p, a, s) : launch_aa_tma<DT, true, false>(p, a, s))
+                        : (p.acc ? launch_aa_tma<DT, false, true>(p, a, s) : launch_aa_tma<DT, false, false>(p, a, s));
+    if (e != cudaErrorNotSupported) return e;
+  }
+  if constexpr (is16(DT)) {                          // no tensor maps: the same step from the lattice
     using Cfg = StepCfg<4, 8>;
     const dim3 grid((unsigned)((p.g.nseg_x + 1) / 2), (unsigned)((p.g.ny + Cfg::WY - 1) / Cfg::WY), (unsigned)p.g.nz);
     const dim3 block(32, Cfg::WY);
