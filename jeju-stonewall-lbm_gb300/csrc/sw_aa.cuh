@@ -325,14 +325,20 @@ __device__ __forceinline__ void aa_pair_even_fast(const StepParams &p, int x0, i
 
 // The collision and scatter of an interior odd-step cell pair (see
 // aa_pair_odd_interior), with the old float64 sums of the pair in acc_old.
+// inlet (lane 0 of the first segment pair, cell x0 = 0): that cell does not
+// pull (v holds its rest state) and scatters its inlet equilibrium
+// (lbm3d.py:67-71) instead of its collision, to the targets that exist and
+// are fluid (those in column 0 need not be: only cells of column 1 pull
+// from column 0).
 template <int DT, bool ACC>
-__device__ __forceinline__ void aa_pair_collide_scatter(const StepParams &p, const f2 (&v)[Q], int x0, int c,
-                                                        int off_ym, int off_yp, int lev, int lane,
+__device__ __forceinline__ void aa_pair_collide_scatter(const StepParams &p, const f2 (&v)[Q], int x0, int c, int z,
+                                                        int off_ym, int off_yp, int lev, int lane, bool inlet,
                                                         const double2 (&acc_old)[4]) {
   using S = Store<DT>;
   using T = typename S::T;
   using PK = Pack16<DT>;
   const Phys<float> ph = phys<float>(p);
+  const float u0 = inlet ? __ldg(p.uin + z) : 0.0f;
   f2 rho, ux, uy, uz;
   collide2(v, x0, true, ph.nu0, ph.c18, p.x_sponge, ph.sponge_scale, ph.nu_sponge, rho, ux, uy, uz, p.status,
            [&](auto I, f2 o) {
@@ -340,8 +346,17 @@ __device__ __forceinline__ void aa_pair_collide_scatter(const StepParams &p, con
              constexpr int ex = CX(k), ey = CY(k), ez = CZ(k);
              T *plane = p.template out<T>(k);
              const int t = c + (ey == 1 ? off_yp : ey == -1 ? off_ym : 0) + ez * lev;   // target row, column x0
+             if (inlet) {                                              // the inlet cell's equilibrium
+               float cu = 0.0f;
+               if constexpr (ex != 0) cu = (ex > 0 ? u0 : -u0);
+               cu = 3.0f * cu;
+               const float w = W<float>(k) * 1.0f * (1.0f + cu + 0.5f * cu * cu - 1.5f * (u0 * u0));
+               o.v.x = w - W<float>(k);
+             }
              if constexpr (ex == 0) {
-               *reinterpret_cast<uint32_t *>(plane + chk(p, t)) = PK::pack(o.v.x, o.v.y);
+               const int tw = chk(p, t);
+               if (!inlet || p.flag[tw] == 0) *reinterpret_cast<uint32_t *>(plane + tw) = PK::pack(o.v.x, o.v.y);
+               else plane[tw + 1] = S::from_shifted(o.v.y);            // column 0's target is not fluid
              } else {
                // targets x0 + ex (first cell) and x0 + 1 + ex (second cell); lane L writes the
                // word holding its second target and lane L + 1's first
@@ -349,15 +364,18 @@ __device__ __forceinline__ void aa_pair_collide_scatter(const StepParams &p, con
                const int w = chk(p, t + (ex == 1 ? 2 : 0));
                if (lane < 31) *reinterpret_cast<uint32_t *>(plane + w) = PK::pack(o.v.y, nxt);
                else plane[w] = S::from_shifted(o.v.y);                 // the other half is the next warp's
-               if (lane == 0) plane[chk(p, t + (ex == 1 ? 1 : -1))] = S::from_shifted(o.v.x);   // the previous warp's
+               if (lane == 0 && !(inlet && ex == -1))                  // the previous warp's (none left of the inlet)
+                 plane[chk(p, t + (ex == 1 ? 1 : -1))] = S::from_shifted(o.v.x);
              }
            });
   if (ACC) {
     const double2 v0 = acc_old[0], v1 = acc_old[1], v2 = acc_old[2], v3 = acc_old[3];
-    *reinterpret_cast<double2 *>(p.accp(0) + c) = make_double2(v0.x + (double)rho.v.x, v0.y + (double)rho.v.y);
-    *reinterpret_cast<double2 *>(p.accp(1) + c) = make_double2(v1.x + (double)ux.v.x, v1.y + (double)ux.v.y);
-    *reinterpret_cast<double2 *>(p.accp(2) + c) = make_double2(v2.x + (double)uy.v.x, v2.y + (double)uy.v.y);
-    *reinterpret_cast<double2 *>(p.accp(3) + c) = make_double2(v3.x + (double)uz.v.x, v3.y + (double)uz.v.y);
+    const double ra = inlet ? 1.0 : (double)rho.v.x, xa = inlet ? (double)u0 : (double)ux.v.x;
+    const double ya = inlet ? 0.0 : (double)uy.v.x, za = inlet ? 0.0 : (double)uz.v.x;
+    *reinterpret_cast<double2 *>(p.accp(0) + c) = make_double2(v0.x + ra, v0.y + (double)rho.v.y);
+    *reinterpret_cast<double2 *>(p.accp(1) + c) = make_double2(v1.x + xa, v1.y + (double)ux.v.y);
+    *reinterpret_cast<double2 *>(p.accp(2) + c) = make_double2(v2.x + ya, v2.y + (double)uy.v.y);
+    *reinterpret_cast<double2 *>(p.accp(3) + c) = make_double2(v3.x + za, v3.y + (double)uz.v.y);
   }
 }
 
@@ -409,7 +427,7 @@ __device__ __forceinline__ void aa_pair_odd_interior(const StepParams &p, int x0
       v[i] = F2(own.y, lane == 31 ? edge[i] : PK::lo(next));
     }
   });
-  aa_pair_collide_scatter<DT, ACC>(p, v, x0, c, off_ym, off_yp, lev, lane, acc_old);
+  aa_pair_collide_scatter<DT, ACC>(p, v, x0, c, z, off_ym, off_yp, lev, lane, false, acc_old);
 }
 
 // Grid: (ceil(pitch / 64), ceil(ny / WY), nz); warp = two adjacent row segments.
@@ -457,10 +475,11 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
 // The AA steps with their sources staged in shared memory by TMA, as k_step_tma
 // does for the two-lattice step (one item of 4 rows x 64 cells per block, all
 // copies issued at the start, bounded waits).  Odd step: the boxes are the
-// two-lattice step's (natural planes at the source rows and levels); an
-// interior warp (not the inlet or outlet segment pair, not the top level, not
-// next to stones or the ground) pulls from them and scatters as
-// aa_pair_odd_interior does; the other warps run the per-cell odd step.  Even
+// two-lattice step's (natural planes at the source rows and levels); a warp
+// not in the outlet segment pair, not at the top level and not next to stones
+// or the ground pulls from them and scatters as aa_pair_odd_interior does (the
+// inlet cell of the first pair scatters its equilibrium); the other warps run
+// the per-cell odd step.  Even
 // step: box i is plane opp(i) -- slot i -- at the item's own rows and level;
 // every warp not next to stones or the ground collides from it as
 // aa_pair_even_fast does.  In place and race-free: every value a cell uses
@@ -525,7 +544,8 @@ __global__ void __launch_bounds__(128, 9)
         const double2 *acc_box = reinterpret_cast<const double2 *>(smem + kTmaStageBytes) + w * 32 + lane;
         pair_collide_store<DT, ACC>(p, v, x0, c, z, x0 == 0, has_b, [&](int k) { return acc_box[k * 4 * 32]; });
       }
-    } else if (!((ka | kb) & TILE_CHECK) && x0s > 0 && x0s + 2 * SEG < g.nx && z < g.nz - 1) {   // odd, interior
+    } else if (!((ka | kb) & TILE_CHECK) && x0s + 2 * SEG < g.nx && z < g.nz - 1) {   // odd: not the outlet or top
+      const bool inlet = x0 == 0;                                     // lane 0 of the first pair
       const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
       const int off_ym = (y == 0) ? (g.ny - 1) * row : -row;
       const int off_yp = (y == g.ny - 1) ? -(g.ny - 1) * row : row;
@@ -548,6 +568,7 @@ __global__ void __launch_bounds__(128, 9)
         } else {                                                      // sources x0 + 1, x0 + 2
           v[i] = F2(PK::hi(own), PK::lo(r[lane_word + 1]));
         }
+        if (inlet) v[i].v.x = 0.0f;                                   // the inlet cell does not pull
       });
       double2 acc_old[4];
       if (ACC) {
@@ -555,7 +576,7 @@ __global__ void __launch_bounds__(128, 9)
 #pragma unroll
         for (int k = 0; k < 4; ++k) acc_old[k] = acc_box[k * 4 * 32];
       }
-      aa_pair_collide_scatter<DT, ACC>(p, v, x0, c, off_ym, off_yp, lev, lane, acc_old);
+      aa_pair_collide_scatter<DT, ACC>(p, v, x0, c, z, off_ym, off_yp, lev, lane, inlet, acc_old);
     } else {                                                          // per cell (from the lattice)
       float fxw = 0.0f, fzw = 0.0f;
       int hit = 0;

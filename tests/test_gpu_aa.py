@@ -75,6 +75,27 @@ def test_aa_equals_two_lattice_step(dtype, cuda):
     np.testing.assert_allclose(ma[1:], mb[1:], rtol=0, atol=u_tol)
 
 
+@pytest.mark.parametrize("dtype", ["f16", "bf16"])
+def test_aa_open_inlet_pairs_equal_two_lattice_step(dtype, cuda):
+    """Stones only mid-channel, nx = 200: the 16-bit odd step's first segment pairs (inlet column
+    included) and its interior pairs take the two-cell path, not the per-cell one."""
+    from gpu_helpers import inlet, make_mask
+    flag = make_mask(200, 12, 13, 6, x_lo=90, x_hi=110, extras=False)
+    uin = inlet(13, 3)
+    ab, aa = _pair(flag, uin, 30, 10, dtype)
+    for n in (2, 4, 24):                        # states are read after even steps
+        ab.advance(n)
+        aa.advance(n)
+        a, b = aa.state_numpy(np.float32), ab.state_numpy(np.float32)
+        fluid = np.broadcast_to(flag == 0, a.shape)
+        np.testing.assert_array_equal(a[~fluid], b[~fluid])
+        _close(a[:, flag == 0], b[:, flag == 0], dtype, f"state after {aa.t} steps")
+    tol = {"f16": (2e-4, 1e-4), "bf16": (1.6e-3, 8e-4)}[dtype]
+    sa, sb = aa.sums(), ab.sums()
+    np.testing.assert_allclose(sa[0], sb[0], rtol=0, atol=aa.n_acc * tol[0])
+    np.testing.assert_allclose(sa[1:], sb[1:], rtol=0, atol=aa.n_acc * tol[1])
+
+
 def test_aa_f32_matches_oracle(cuda, oracle_mod):
     """Ten in-place steps against ten steps of the CPU restatement of the reference kernel."""
     from gpu_helpers import assert_fields_close, assert_force_close, inlet, make_mask
