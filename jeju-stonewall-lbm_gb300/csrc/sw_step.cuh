@@ -525,8 +525,8 @@ __device__ __forceinline__ void collide2(const f2 (&f)[Q], int x0, bool has_b, f
 // warp covers 64 cells of a row.  Pulls along x take the neighbouring cell's
 // half from the adjacent lane (warp shuffle); the first and last lane load the
 // cell just outside the warp's 64 directly.  Outputs are packed two per 32-bit
-// store.  Warps whose segments need flag tests run the per-cell path for both
-// of their cells.
+// store.  Warps whose segments need flag tests take the same two-cell path with
+// the link masks of their cells (pair_links_prefetch, pair_link).
 template <int DT> struct Pack16;
 template <> struct Pack16<SW_F16_SHIFT> {
   static __device__ __forceinline__ float2 both(uint32_t v) {

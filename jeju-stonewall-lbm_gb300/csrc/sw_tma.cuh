@@ -1,7 +1,7 @@
 // sw_tma.cuh -- the 16-bit step with its pull sources staged in shared memory by TMA.
 //
 // Included by sw_step.cuh after the cell code it reuses (collide2, Pack16,
-// step_cell, warp_force_add).  Same cells, same arithmetic, same results as
+// the link masks of the checked path, warp_force_add).  Same cells, same arithmetic, same results as
 // the two-cells-per-thread kernel (k_step_pair); what changes is how the 19
 // pulled values reach the registers.  k_step_pair loads every population row
 // with 32-bit loads and moves the x-shifted ones between lanes (shuffles plus
