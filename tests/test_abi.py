@@ -125,3 +125,24 @@ def test_native_unavailable_is_loud(monkeypatch, tmp_path):
     monkeypatch.setattr(N, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(N.NativeUnavailable):
         N.lib()
+
+
+def test_recirculation_box_matches_the_host_slices(native_lib):
+    """sw_recirc_scratch_bytes sizes the box that recirculation_area (export3d.py:177-179) slices
+    out of the every-2nd-cell field: i in [X0 // 2, min(ceil(nx / 2), (X0 + 10 H) // 2)), every j,
+    k < min(ceil(nz / 2), 2 H // 2); empty or one-level boxes are refused."""
+    from stonewall import _native as N
+    rng = np.random.default_rng(11)
+    for _ in range(300):
+        nx, ny, nz = (int(v) for v in rng.integers(2, 400, 3))
+        H, X0 = int(rng.integers(1, 60)), int(rng.integers(0, 500))
+        g = N.geom(nx, ny, nz)
+        shape = [len(range(n)[::2]) for n in (nx, ny, nz)]          # the every-2nd-cell field
+        i0, i1 = X0 // 2, min(shape[0], (X0 + 10 * H) // 2)
+        k1 = min(shape[2], int(2 * H) // 2)
+        sub = (len(range(shape[0])[i0:i1]), shape[1], len(range(shape[2])[:k1]))   # ux[i0:i1, :, :k1]
+        got = native_lib.sw_recirc_scratch_bytes(ctypes.byref(g), H, X0)
+        if np.prod(sub) == 0 or sub[2] < 2:
+            assert got == N.SW_ERR_BAD_ARG, (nx, ny, nz, H, X0)
+        else:
+            assert got == 2 * int(np.prod(sub)) * 4, (nx, ny, nz, H, X0)
