@@ -479,10 +479,11 @@ __global__ void __launch_bounds__(Cfg::THREADS, Cfg::MINB)
 // not in the outlet segment pair, not at the top level and not next to stones
 // or the ground pulls from them and scatters as aa_pair_odd_interior does (the
 // inlet cell of the first pair scatters its equilibrium); the other warps run
-// the per-cell odd step.  Even
-// step: box i is plane opp(i) -- slot i -- at the item's own rows and level;
-// every warp not next to stones or the ground collides from it as
-// aa_pair_even_fast does.  In place and race-free: every value a cell uses
+// the per-cell odd step.  Even step: box i is plane opp(i) -- slot i -- at
+// the item's own rows and level; every warp collides from it as
+// aa_pair_even_fast does, warps next to stones or the ground with the link
+// masks of their cells (the stone links' force, cells that are not fluid left
+// unwritten).  In place and race-free: every value a cell uses
 // from a box is written in this step only by that cell, after its wait; the
 // rest of a box (columns and rows of neighbouring items) may be read while
 // its owners rewrite it, and is not used.
@@ -528,11 +529,55 @@ __global__ void __launch_bounds__(128, 9)
     kb = sa + 1 < g.nseg_x ? __ldg(p.tiles + seg + 1) : (uint8_t)TILE_ALL_SOLID;
   }
   __syncthreads();
+  // even step next to stones or the ground: the link masks of the lane's cells
+  // (which cells are fluid, which links come from stones), fetched during the copies
+  const bool even_checked = !ODD && y < g.ny && !(ka & kb & TILE_ALL_SOLID) && ((ka | kb) & TILE_CHECK);
+  uint32_t sm[2] = {1u, 1u}, wm[2] = {0u, 0u};
+  if (even_checked) {
+    cell_links(p, x0, y, z, sm[0], wm[0]);
+    cell_links(p, x0 + 1, y, z, sm[1], wm[1]);
+  }
   bool ok = mbar_wait(smem_u32(&bar), 0u, p.tma_poll_limit);
   if (ok && y < g.ny && !(ka & kb & TILE_ALL_SOLID)) {
     const int row = g.pitch, lev = g.ny * g.pitch;
     const int lane_word = 4 + lane;                                   // 32-bit word of elements 8 + 2 lane, + 1
-    if (!((ka | kb) & TILE_CHECK) && !ODD) {                          // even step: own slots, local
+    if (even_checked) {
+      // The even step reads the cell's own slots, where the odd step already put the
+      // bounce-back values (rule (d)); a link from a stone adds -2 (f - w) c of its
+      // value to the wall force (lbm3d.py:91-101), cell x0 before x0 + 1, as
+      // aa_even_cell adds them; cells that are not fluid are not stored.
+      float fxw = 0.0f, fzw = 0.0f;
+      int hit = 0;
+      if (x0 < g.nx) {
+        const bool has_b = x0 + 1 < g.nx;
+        const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
+        f2 v[Q];
+        static_for<0, Q>([&](auto I) {
+          constexpr int i = decltype(I)::value;
+          v[i].v = PK::both(reinterpret_cast<const uint32_t *>(smem + i * kTmaBoxBytes + w * kTmaRowBytes)[lane_word]);
+        });
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          static_for<1, Q>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            constexpr int ex = CX(i), ez = CZ(i);
+            if ((wm[h] >> i) & 1u) {
+              const float fr = h ? v[i].v.y : v[i].v.x;
+              if constexpr (ex != 0) fxw = fxw - 2.0f * fr * (float)ex;
+              if constexpr (ez != 0) fzw = fzw - 2.0f * fr * (float)ez;
+              hit = 1;
+            }
+          });
+        }
+        const uint32_t keep = pair_solid_cells(v, sm);
+        if (keep != 0u) {
+          const double2 *acc_box = reinterpret_cast<const double2 *>(smem + kTmaStageBytes) + w * 32 + lane;
+          pair_collide_store<DT, ACC, true>(p, v, x0, c, z, x0 == 0, has_b,
+                                            [&](int k) { return acc_box[k * 4 * 32]; }, keep);
+        }
+      }
+      if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
+    } else if (!((ka | kb) & TILE_CHECK) && !ODD) {                   // even step: own slots, local
       if (x0 < g.nx) {
         const bool has_b = x0 + 1 < g.nx;
         const int c = chk(p, (z * g.ny + y) * g.pitch + x0);
@@ -580,14 +625,9 @@ __global__ void __launch_bounds__(128, 9)
     } else {                                                          // per cell (from the lattice)
       float fxw = 0.0f, fzw = 0.0f;
       int hit = 0;
-      if ((ka | kb) & TILE_CHECK) {
-        if (ODD) {
-          if (x0 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0, y, z, fxw, fzw, hit);
-          if (x0 + 1 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0 + 1, y, z, fxw, fzw, hit);
-        } else {
-          if (x0 < g.nx) aa_even_cell<DT, true, ACC>(p, x0, y, z, fxw, fzw, hit);
-          if (x0 + 1 < g.nx) aa_even_cell<DT, true, ACC>(p, x0 + 1, y, z, fxw, fzw, hit);
-        }
+      if ((ka | kb) & TILE_CHECK) {                                   // odd step next to stones or the ground
+        if (x0 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0, y, z, fxw, fzw, hit);
+        if (x0 + 1 < g.nx) aa_odd_cell<DT, true, ACC>(p, a, x0 + 1, y, z, fxw, fzw, hit);
         if (((ka | kb) & TILE_FORCE) && p.force != nullptr) warp_force_add<float>(p, z, lane, fxw, fzw, hit);
       } else {                                                        // odd: inlet, outlet, top
         if (x0 < g.nx) aa_odd_cell<DT, false, ACC>(p, a, x0, y, z, fxw, fzw, hit);
