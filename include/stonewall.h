@@ -186,6 +186,12 @@ int sw_status_error(uint32_t word);
  * device fault.  Returns the previous value; a negative argument only reads. */
 int32_t sw_debug_tma_poll_limit(int32_t polls);
 
+/* Test hook, no reference counterpart: 1 (the default) lets 16-bit AA steps
+ * stage their sources by TMA, 0 runs the same steps with plain loads (the form
+ * used when tensor maps cannot be made), so both stay tested.  Returns the
+ * previous value; a negative argument only reads. */
+int32_t sw_debug_aa_tma(int32_t on);
+
 /* AA pattern: the same step on ONE lattice, updated in place (half the
  * memory of f_in + f_out).  No reference counterpart: the reference always
  * steps f0 into f1 (lbm3d.py:293-294, 362); this replaces that pair of

@@ -40,6 +40,7 @@ constexpr int kGhostPops = 5;
 struct AAParams {
   const void *ghost;  // [5][nz][ny] stored values of the outlet plane, before the odd step
   void *ghost_w;      // same buffer, written by k_aa_ghost
+  int tma = 1;        // 16-bit storage: stage the sources by TMA when the tensor maps can be made
 };
 
 // Outlet plane's c_x = -1 populations -> ghost.  One thread per (y, z).
@@ -685,9 +686,11 @@ cudaError_t launch_aa(const StepParams &p_in, const AAParams &a, bool odd, cudaS
     if (e != cudaSuccess) return e;
   }
   if constexpr (is16(DT)) {                          // two cells per thread, sources staged by TMA
-    cudaError_t e = odd ? (p.acc ? launch_aa_tma<DT, true, true>(p, a, s) : launch_aa_tma<DT, true, false>(p, a, s))
+    if (a.tma) {
+      cudaError_t e = odd ? (p.acc ? launch_aa_tma<DT, true, true>(p, a, s) : launch_aa_tma<DT, true, false>(p, a, s))
                         : (p.acc ? launch_aa_tma<DT, false, true>(p, a, s) : launch_aa_tma<DT, false, false>(p, a, s));
-    if (e != cudaErrorNotSupported) return e;
+      if (e != cudaErrorNotSupported) return e;
+    }
   }
   if constexpr (is16(DT)) {                          // no tensor maps: the same step from the lattice
     using Cfg = StepCfg<4, 8>;

@@ -232,6 +232,15 @@ int sw_status_error(uint32_t word) {
   return SW_OK;
 }
 
+// whether 16-bit AA steps stage their sources by TMA (sw_debug_aa_tma)
+int g_aa_tma = 1;
+
+int32_t sw_debug_aa_tma(int32_t on) {
+  const int32_t old = g_aa_tma;
+  if (on >= 0) g_aa_tma = on != 0;
+  return old;
+}
+
 int32_t sw_debug_tma_poll_limit(int32_t polls) {
   const int32_t old = g_tma_poll_limit;
   if (polls >= 0) g_tma_poll_limit = polls;
@@ -364,7 +373,7 @@ int sw_step_aa(const sw_geom *g, int dtype, void *f, int32_t odd, const uint8_t 
   p.status = status;
   p.cfg = 0;
   p.tma_poll_limit = g_tma_poll_limit;
-  sw::AAParams a{ghost, ghost};
+  sw::AAParams a{ghost, ghost, g_aa_tma};
   clear_stale();
   cudaError_t e;
   switch (dtype) {

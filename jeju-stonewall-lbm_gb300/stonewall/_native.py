@@ -104,6 +104,7 @@ def load(path):
                             ctypes.c_int),
         "sw_status_error": ([ctypes.c_uint32], ctypes.c_int),
         "sw_debug_tma_poll_limit": ([i32], i32),
+        "sw_debug_aa_tma": ([i32], i32),
         "sw_step_config_count": ([], ctypes.c_int),
         "sw_set_step_config": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "sw_get_step_config": ([ctypes.c_int], ctypes.c_int),

@@ -146,3 +146,12 @@ def test_recirculation_box_matches_the_host_slices(native_lib):
             assert got == N.SW_ERR_BAD_ARG, (nx, ny, nz, H, X0)
         else:
             assert got == 2 * int(np.prod(sub)) * 4, (nx, ny, nz, H, X0)
+
+
+def test_aa_tma_hook_reads_and_restores(native_lib):
+    L = native_lib
+    assert L.sw_debug_aa_tma(-1) == 1                   # read only: staged by default
+    assert L.sw_debug_aa_tma(0) == 1
+    assert L.sw_debug_aa_tma(-1) == 0
+    assert L.sw_debug_aa_tma(5) == 0                    # any non-zero value switches it on
+    assert L.sw_debug_aa_tma(-1) == 1

@@ -96,6 +96,27 @@ def test_aa_open_inlet_pairs_equal_two_lattice_step(dtype, cuda):
     np.testing.assert_allclose(sa[1:], sb[1:], rtol=0, atol=aa.n_acc * tol[1])
 
 
+@pytest.mark.parametrize("dtype", ["f16", "bf16"])
+def test_aa_without_tma_staging_equals_two_lattice_step(dtype, cuda):
+    """The 16-bit AA steps with plain loads (the form used when no tensor maps can be made)."""
+    from gpu_helpers import inlet, make_mask
+    from stonewall import _native as N
+    L = N.lib()
+    old = L.sw_debug_aa_tma(0)
+    try:
+        for flag in (make_mask(45, 10, 13, 5), make_mask(200, 12, 13, 6, x_lo=90, x_hi=110, extras=False)):
+            ab, aa = _pair(flag, inlet(13, 3), 24, 6, dtype)
+            for n in (2, 22):
+                ab.advance(n)
+                aa.advance(n)
+                a, b = aa.state_numpy(np.float32), ab.state_numpy(np.float32)
+                fluid = np.broadcast_to(flag == 0, a.shape)
+                np.testing.assert_array_equal(a[~fluid], b[~fluid])
+                _close(a[:, flag == 0], b[:, flag == 0], dtype, f"state after {aa.t} steps")
+    finally:
+        L.sw_debug_aa_tma(old)
+
+
 def test_aa_f32_matches_oracle(cuda, oracle_mod):
     """Ten in-place steps against ten steps of the CPU restatement of the reference kernel."""
     from gpu_helpers import assert_fields_close, assert_force_close, inlet, make_mask
