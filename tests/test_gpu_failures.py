@@ -81,6 +81,41 @@ def test_nonfinite_density_in_the_aa_step(dtype, cuda):
         assert status.read() == want
 
 
+def test_aa_tma_timeout_is_reported_and_the_context_stays_usable(cuda):
+    """Poll limit 0 on the TMA-staged 16-bit AA steps: both step kinds report SW_STATUS_TIMEOUT and the
+    blocks' copies land before they leave; with the limit restored an AA pair of steps from a fresh
+    state equals a clean run."""
+    import torch
+    from stonewall import _native as N
+    from stonewall.fields import Flags, Grid, Lattice, StatusWord
+    from stonewall.kernels import DeviceVector, k_step_aa
+    L = N.lib()
+    flag, uin, f0 = _case(3, (96, 16, 17))
+    g = Grid(*flag.shape)
+    flags, uv = Flags(g, flag), DeviceVector(uin)
+    ghost = torch.empty(L.sw_aa_ghost_elems(g.gp) * 2, dtype=torch.uint8, device="cuda")
+
+    def two_steps():
+        f, status = Lattice(g, "f16").assign(f0), StatusWord()
+        for t in range(2):
+            k_step_aa(f, t == 0, flags, uv, 2e-3, 0.1, 86, 0.05, None, t, ghost=ghost, status=status)
+        return status.read(), f.numpy(np.float64)
+
+    word0, ref = two_steps()
+    assert word0 == 0
+    L.sw_tma_timeouts()                                  # clear the counter
+    old = L.sw_debug_tma_poll_limit(0)
+    try:
+        word, _ = two_steps()
+        blocks = L.sw_tma_timeouts()
+    finally:
+        L.sw_debug_tma_poll_limit(old)
+    assert word & N.SW_STATUS_TIMEOUT and blocks > 0
+    word2, again = two_steps()
+    assert word2 == 0 and L.sw_tma_timeouts() == 0
+    np.testing.assert_array_equal(again, ref)
+
+
 def test_tma_timeout_is_reported_and_the_context_stays_usable(cuda):
     """Poll limit 0: every TMA-staged block gives up at its first stage.  The status word and the
     process-wide counter report it, the autotuner drops the configuration, and with the limit
