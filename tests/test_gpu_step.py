@@ -218,3 +218,14 @@ def test_gaussian_init_matches_oracle(cuda, oracle_mod):
     k_init(f, Flags(grid, flag), DeviceVector(uin), 0.02, 9, "gauss")
     want = oracle_mod.init(flag, uin, noise=np.float32(0.02), seed=9, noise_kind=1)
     np.testing.assert_allclose(f.numpy(), want, rtol=2e-6, atol=0)
+
+
+def test_stepbench_times_every_form(capsys, cuda):
+    """The kernel-timing tool runs the two-lattice configurations it is given and the AA steps."""
+    import json
+    from stonewall import stepbench
+    stepbench.main(["--H", "8", "--cfgs", "0,4,10", "--reps", "2", "--aa"])
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert out["grid"] == [160, 32, 32] and out["dtype"] == "f16"
+    assert set(out["ms"]) == {"0", "0a", "4", "4a", "10", "10a", "aa_odd", "aa_even", "aa_odda", "aa_evena"}
+    assert all(v > 0 for v in out["ms"].values())
