@@ -58,3 +58,43 @@ def test_aa_plan_on_generated_masks():
         np.testing.assert_allclose(got[fluid], want[fluid], rtol=1e-12, atol=1e-12)
 
     check()
+
+
+def _segment_checked(flag, x_lo, x_hi, y, z):
+    """k_build_tiles' CHECK class of the cells x_lo..x_hi-1 of row (y, z): a cell is not fluid, or a
+    fluid cell past the inlet has a pull source that is not fluid (lbm3d.py:77-95)."""
+    from aa_model import pull_source
+    nx = flag.shape[0]
+    for x in range(x_lo, min(x_hi, nx)):
+        if flag[x, y, z] != 0:
+            return True
+        if x > 0 and any(pull_source(flag, x, y, z, i)[2] for i in range(1, 19)):
+            return True
+    return False
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_inlet_cell_targets_of_open_first_pairs(seed):
+    """The 16-bit odd step runs the first 64-cell pair of a row on the two-cell path when neither of
+    its segments is checked; its inlet cell then writes its c_x = +1 populations to column 1 without
+    a flag test.  Those targets are pull sources of the row's x = 1 cell, so they are fluid."""
+    from aa_model import C, odd_targets
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = 70, 24, 9
+    flag = (rng.random((nx, ny, nz)) < 0.0005 * (1 + seed)).astype(np.uint8)
+    for _ in range(6):                                   # stones in columns 0 and 1 next to open rows
+        flag[int(rng.integers(0, 2)), int(rng.integers(0, ny)), int(rng.integers(1, nz))] = 1
+    flag[:, :, 0] = 2
+    open_rows = 0
+    for y in range(ny):
+        for z in range(1, nz - 1):
+            if flag[0, y, z] != 0 or _segment_checked(flag, 0, 32, y, z) or _segment_checked(flag, 32, 64, y, z):
+                continue
+            open_rows += 1
+            for k in range(19):
+                if C[k][0] != 1:
+                    continue
+                t = (1, (y + C[k][1]) % ny, z + C[k][2])
+                assert flag[t] == 0, (y, z, k, t)
+                assert (k, t) in odd_targets(flag, (0, y, z), k)
+    assert open_rows > 0
