@@ -244,6 +244,9 @@ typedef struct sw_batch_entry {
   int64_t t0;            /* step index of launch k = 0 */
   int64_t steps_left;    /* launches with k >= steps_left leave the lattice untouched */
   uint32_t *status;      /* the lattice's device status word (SW_STATUS_*), or NULL: no checks */
+  void *ghost;           /* NULL: the two-lattice pattern.  Otherwise an in-place AA member (graph mode
+                          * only): f[0] == f[1] is its one lattice, ghost its sw_aa_ghost_elems buffer,
+                          * and cur0 = 0 when its next step is odd, 1 when even */
 } sw_batch_entry;
 
 typedef struct sw_batch_header {
@@ -280,8 +283,10 @@ int sw_batch_step(const sw_batch_header *hdr_dev, const sw_batch_entry *table_de
  * handle's executable graph (instantiating anew only when the number of
  * lattices or launches changed) and launches it on s; the handle's two
  * executable graphs alternate, so a call may wait for the launch of the call
- * before last to finish.  One handle per device and host thread.  No
- * reference counterpart (see sw_batch_step). */
+ * before last to finish.  Entries with a ghost buffer are in-place AA
+ * members: their chains alternate sw_step_aa odd and even steps (odd first
+ * when cur0 = 0).  One handle per device and host thread.  No reference
+ * counterpart (see sw_batch_step). */
 #define SW_BATCH_MAX_ENTRIES 256
 typedef struct sw_batch_graph sw_batch_graph;
 int sw_batch_graph_create(sw_batch_graph **out);

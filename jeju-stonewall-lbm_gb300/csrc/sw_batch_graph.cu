@@ -7,7 +7,9 @@
 // parameters and the hardware block scheduler), and the chains are captured
 // on separate streams, so they are parallel branches of one graph between a
 // fork and a join: lattices run concurrently and the GPU fills the tail of one
-// lattice's step with blocks of another's.  The graph is captured again for
+// lattice's step with blocks of another's.  A member on the in-place AA
+// pattern (entry.ghost set) gets a chain of alternating odd and even
+// sw_step_aa launches instead.  The graph is captured again for
 // every call (the step index, force row and buffer parity of each launch are
 // kernel parameters) and swapped into an executable graph with
 // cudaGraphExecUpdate, which keeps the instantiation when the shape (lattices
@@ -104,6 +106,7 @@ int sw_batch_graph_run(sw_batch_graph *g, const sw_batch_entry *entries, int32_t
   for (int i = 0; i < n; ++i) {
     const sw_batch_entry &b = entries[i];
     if (!b.f[0] || !b.f[1] || b.cur0 < 0 || b.cur0 > 1 || b.t0 < 0 || b.steps_left < 0) return SW_ERR_BAD_ARG;
+    if ((b.ghost != nullptr) != (b.f[0] == b.f[1])) return SW_ERR_BAD_ARG;    // in place exactly for AA members
     if (b.acc && b.acc_every <= 0) return SW_ERR_BAD_ARG;
   }
   e = ensure_branches(g, n);
@@ -123,9 +126,13 @@ int sw_batch_graph_run(sw_batch_graph *g, const sw_batch_entry *entries, int32_t
       const long long t = b.t0 + k;
       const int cur = (b.cur0 + k) & 1;
       sw_stream bs = reinterpret_cast<sw_stream>(g->branch[i]);
-      // the storage type's installed configuration (plain or accumulating), checks into b.status
-      rc = sw_step_checked(&b.geom, dtype, b.f[cur], b.f[cur ^ 1], b.flag, b.tiles, b.uin, b.nu0, b.cs, b.x_sponge,
-                           b.nu_sponge, b.force, t, accumulates(b, t) ? b.acc : nullptr, -1, b.status, bs);
+      if (b.ghost)                                    // in place: odd and even AA steps alternate
+        rc = sw_step_aa(&b.geom, dtype, b.f[0], cur == 0, b.flag, b.tiles, b.uin, b.nu0, b.cs, b.x_sponge,
+                        b.nu_sponge, b.force, t, accumulates(b, t) ? b.acc : nullptr, b.ghost, b.status, bs);
+      else                                            // the storage type's installed configuration
+        rc = sw_step_checked(&b.geom, dtype, b.f[cur], b.f[cur ^ 1], b.flag, b.tiles, b.uin, b.nu0, b.cs,
+                             b.x_sponge, b.nu_sponge, b.force, t, accumulates(b, t) ? b.acc : nullptr, -1, b.status,
+                             bs);
       ++launches;
     }
   }

@@ -3,6 +3,7 @@
 // Every entry point validates its arguments, launches on the caller's stream
 // and returns an SW_* status; nothing here allocates or synchronises.
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 
 #include "sw_aa.cuh"
@@ -292,6 +293,12 @@ int sw_macro_accum(const sw_geom *g, int dtype, const void *f, const uint8_t *fl
   return cuda_status(sw::aux_macro(to_geom(g), dtype, f, flag, u, acc, st(s)));
 }
 
+// The table layout the Python host mirrors (stonewall/batch.py).
+static_assert(sizeof(sw_batch_entry) == 160 && offsetof(sw_batch_entry, status) == 144 &&
+                  offsetof(sw_batch_entry, ghost) == 152 && offsetof(sw_batch_entry, t0) == 128,
+              "sw_batch_entry layout");
+static_assert(sizeof(sw_batch_header) == 32 && offsetof(sw_batch_header, next_item) == 16, "sw_batch_header layout");
+
 int sw_batch_prepare(sw_batch_entry *entries, int32_t n, int dtype, int cfg, sw_batch_header *hdr) {
   if (!entries || n <= 0 || !hdr || !dtype_ok(dtype)) return SW_ERR_BAD_ARG;
   if (cfg < 0 || cfg >= sw::kStepConfigs) return SW_ERR_BAD_ARG;
@@ -302,6 +309,7 @@ int sw_batch_prepare(sw_batch_entry *entries, int32_t n, int dtype, int cfg, sw_
   long long item0 = 0;
   for (int i = 0; i < n; ++i) {
     sw_batch_entry &e = entries[i];
+    if (e.ghost) return SW_ERR_UNSUPPORTED;                          // AA members: graph mode only
     if (!geom_ok(&e.geom) || !e.f[0] || !e.f[1] || e.f[0] == e.f[1] || !aligned16(e.f[0]) || !aligned16(e.f[1]))
       return SW_ERR_BAD_ARG;
     if (!e.flag || !e.tiles || !e.uin || e.cur0 < 0 || e.cur0 > 1 || e.t0 < 0) return SW_ERR_BAD_ARG;

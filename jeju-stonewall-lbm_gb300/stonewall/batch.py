@@ -16,7 +16,8 @@ include/stonewall.h).  Two modes advance the table:
       composition keeps its shape.
 
 autotune() times both and keeps the faster.  All members share one storage
-type.
+type.  Members on the in-place AA pattern (half the memory of a wall) run in
+graph mode, as chains of alternating odd and even in-place steps.
 
 A member's results do not depend on the others (cells are owned by one
 thread, wall forces are integer sums), so a wall gives the same bits alone
@@ -38,7 +39,7 @@ class SwBatchEntry(ctypes.Structure):
                 ("nu0", ctypes.c_double), ("cs", ctypes.c_double), ("nu_sponge", ctypes.c_double),
                 ("x_sponge", ctypes.c_int32), ("n_spin", ctypes.c_int32), ("acc_every", ctypes.c_int32),
                 ("cur0", ctypes.c_int32), ("t0", ctypes.c_int64), ("steps_left", ctypes.c_int64),
-                ("status", ctypes.c_void_p)]
+                ("status", ctypes.c_void_p), ("ghost", ctypes.c_void_p)]
 
 
 class SwBatchHeader(ctypes.Structure):
@@ -125,10 +126,12 @@ class Batch:
 
     # ------------------------------------------------------------ membership
     def add(self, solver):
+        """Add a WallSolver.  Members on the in-place AA pattern (half the memory) run in graph mode
+        only: their chains alternate the odd and even in-place steps."""
         if solver.dtype != self.dtype:
             raise ValueError("all members of a batch share one storage type")
-        if getattr(solver, "pattern", "ab") != "ab":
-            raise ValueError("batch members use the two-lattice pattern")
+        if getattr(solver, "pattern", "ab") == "aa" and self.mode != "graph":
+            raise ValueError("in-place (AA) members need graph mode")
         if len(self.members) >= self.max_members:
             raise RuntimeError("batch is full")
         self.members.append(solver)
@@ -151,8 +154,10 @@ class Batch:
         for i, m in enumerate(live):
             e = tab[i]
             e.geom = m.grid.geom
+            aa = getattr(m, "pattern", "ab") == "aa"
             e.f[0] = m.f[0].data.data_ptr()
-            e.f[1] = m.f[1].data.data_ptr()
+            e.f[1] = m.f[0 if aa else 1].data.data_ptr()
+            e.ghost = m.ghost.data_ptr() if aa else None
             e.flag = m.flags.flag.data_ptr()
             e.tiles = m.flags.tiles.data_ptr()
             e.uin = m.uin.data.data_ptr()
@@ -160,7 +165,8 @@ class Batch:
             e.acc = None if tuning else m.acc.data.data_ptr()
             e.status = (self._scratch_status if tuning else m.status).data.data_ptr()
             e.nu0, e.cs, e.nu_sponge = m.nu0, m.cs, m.nu_sponge
-            e.x_sponge, e.n_spin, e.acc_every, e.cur0 = m.x_sponge, m.n_spin, m.acc_every, m.cur
+            e.x_sponge, e.n_spin, e.acc_every = m.x_sponge, m.n_spin, m.acc_every
+            e.cur0 = (0 if m.aa_odd_next else 1) if aa else m.cur
             e.t0 = m.t
             e.steps_left = min(n_steps, m.n_total - m.t)
         if not live or not upload:
@@ -261,7 +267,10 @@ class Batch:
                 s = min(c, m.n_total - m.t)
                 m.n_acc += acc_steps(m.t, s, m.n_spin, m.acc_every)
                 m.t += s
-                m.cur ^= (s & 1)
+                if getattr(m, "pattern", "ab") == "aa":
+                    m.aa_odd_next ^= bool(s & 1)
+                else:
+                    m.cur ^= (s & 1)
             n -= c
         if check:
             self.check()
@@ -283,6 +292,8 @@ class Batch:
         spare buffer with forces and sums switched off, so the members' states are not changed.
         Returns (best, times): best is a configuration number or "graph"."""
         times = {}
+        if any(getattr(m, "pattern", "ab") == "aa" for m in self.members):
+            return "graph", times                    # in-place members: graph mode, and no trial steps
         if "persistent" in modes:
             for cfg in range(N.lib().sw_step_config_count()):
                 if not _valid(self.dtype, cfg):

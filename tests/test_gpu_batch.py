@@ -14,11 +14,12 @@ from gpu_helpers import inlet, make_mask
 pytestmark = pytest.mark.gpu
 
 
-def _member(shape, seed, n_total, n_spin, dtype):
+def _member(shape, seed, n_total, n_spin, dtype, pattern="ab"):
     from stonewall.solver import WallSolver
     nx, ny, nz = shape
     flag = make_mask(nx, ny, nz, seed)
-    s = WallSolver(flag, inlet(nz, max(2, nz // 4)), 2e-3, 0.1, nx - nx // 5, n_total, n_spin=n_spin, dtype=dtype)
+    s = WallSolver(flag, inlet(nz, max(2, nz // 4)), 2e-3, 0.1, nx - nx // 5, n_total, n_spin=n_spin, dtype=dtype,
+                   pattern=pattern)
     return s.init(noise=0.03, seed=seed, noise_kind="gauss")
 
 
@@ -121,3 +122,32 @@ def test_autotune_keeps_the_states(cuda):
         np.testing.assert_array_equal(m.state.numpy(np.float64), x)
     b.advance(20)
     assert not b.pending()
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16"])
+def test_aa_members_in_graph_mode_equal_their_solo_runs(dtype, cuda):
+    """In-place (AA) members beside two-lattice ones, odd chunk lengths (the odd/even parity carries
+    across chunks): every member ends with the bits of its own solo run."""
+    from stonewall.batch import Batch
+    plan = [(SHAPES[0], "aa", 40), (SHAPES[1], "ab", 40), (SHAPES[2], "aa", 26)]
+    solo = []
+    for (shape, seed), pattern, n in plan:
+        r = _member(shape, seed, n, 9, dtype, pattern)
+        r.advance(n, use_graphs=False)
+        solo.append(_snapshot(r))
+    b = Batch(dtype=dtype, chunk=7, mode="graph")
+    ms = [b.add(_member(shape, seed, n, 9, dtype, pattern)) for (shape, seed), pattern, n in plan]
+    assert b.autotune()[0] == "graph"
+    b.advance(40)
+    assert not b.pending()
+    for want, m in zip(solo, ms):
+        got = _snapshot(m)
+        for u, v in zip(want[:3], got[:3]):
+            np.testing.assert_array_equal(u, v)
+        assert want[3:] == got[3:]
+
+
+def test_aa_members_need_graph_mode(cuda):
+    from stonewall.batch import Batch
+    with pytest.raises(ValueError):
+        Batch(dtype="f16", mode="persistent").add(_member(SHAPES[0][0], 1, 10, 2, "f16", "aa"))

@@ -17,14 +17,16 @@ def test_acc_steps_counts_the_accumulating_steps():
 
 
 def test_batch_entry_matches_the_c_layout():
-    """sw_batch_entry in include/stonewall.h: 152 bytes, the fields at their C offsets."""
+    """sw_batch_entry in include/stonewall.h: 160 bytes, the fields at their C offsets (sw_capi.cu
+    asserts the same sizes and offsets at compile time)."""
     from stonewall.batch import SwBatchEntry, SwBatchHeader
-    assert ctypes.sizeof(SwBatchEntry) == 152
+    assert ctypes.sizeof(SwBatchEntry) == 160
     assert ctypes.sizeof(SwBatchHeader) == 32
     assert SwBatchHeader.next_item.offset == 16 and SwBatchHeader.done_blocks.offset == 24
     off = {name: getattr(SwBatchEntry, name).offset for name, _ in SwBatchEntry._fields_}
     assert off["geom"] == 0 and off["item0"] == 16 and off["f"] == 32 and off["nu0"] == 88
     assert off["x_sponge"] == 112 and off["t0"] == 128 and off["steps_left"] == 136 and off["status"] == 144
+    assert off["ghost"] == 152
 
 
 def test_poisson_requests_are_seeded_and_in_range():
