@@ -80,13 +80,15 @@ def poisson_requests(rate, duration, seed=0, H_range=(16, 48), porosity=(0.0, 0.
         rid += 1
 
 
-def footprint(req):
-    """Device bytes a request holds while resident."""
+def footprint(req, pattern="ab"):
+    """Device bytes a request holds while resident: two lattices (pattern "ab") or one and the
+    outlet ghost (pattern "aa", in place), flags, segment classes, float64 sums, force series."""
     p = baseline_params(req.H, req.steps, UH=req.U)
     pitch = (p.nx + 31) // 32 * 32
     cells = pitch * p.ny * p.nz
-    return (2 * 19 * DTYPE_BYTES[req.dtype] * cells + 32 * cells + cells + cells // 32 + req.steps * p.nz * 16
-            + p.nz * 4)
+    lattices = 2 * 19 * DTYPE_BYTES[req.dtype] * cells if pattern == "ab" else \
+        19 * DTYPE_BYTES[req.dtype] * cells + 5 * p.ny * p.nz * DTYPE_BYTES[req.dtype]
+    return lattices + 32 * cells + cells + cells // 32 + req.steps * p.nz * 16 + p.nz * 4
 
 
 def cells_of(req):
@@ -102,9 +104,9 @@ def prepare(req, mask_device=None):
     return p, flags_from_wall(wall, p.nx, p.ny, p.nz)
 
 
-def make_solver(req, p, flag, device="cuda"):
+def make_solver(req, p, flag, device="cuda", pattern="ab"):
     s = WallSolver(flag, p.uin, p.nu0, p.Cs, p.x_sponge, req.steps, n_spin=p.n_spin, dtype=req.dtype,
-                   device=device)
+                   device=device, pattern=pattern)
     s.init(noise=0.02, seed=req.seed, noise_kind="gauss")
     s.params = p
     return s
@@ -137,7 +139,12 @@ def solve_stats_host(s):
 
 class Server:
     def __init__(self, cap_bytes=160e9, chunk=50, max_members=256, device="cuda", workers=4, clock=time.monotonic,
-                 mode="graph", max_cells=None, check_every=20, mask_device="cuda"):
+                 mode="graph", max_cells=None, check_every=20, mask_device="cuda", pattern="ab"):
+        """pattern "aa": every request is solved in place (one lattice: about half the memory of
+        "ab"), which the graph batch mode runs."""
+        if pattern not in ("ab", "aa") or (pattern == "aa" and mode != "graph"):
+            raise ValueError("pattern is 'ab', or 'aa' with mode 'graph'")
+        self.pattern = pattern
         self.cap = float(cap_bytes)
         self.max_cells = float(max_cells) if max_cells else float("inf")
         self.cells = 0
@@ -172,7 +179,7 @@ class Server:
             fut = prepared.get(req.rid)
             if fut is None or not fut.done():
                 return                               # head still being prepared: keep FIFO order
-            need = footprint(req)
+            need = footprint(req, self.pattern)
             if need > self.cap:
                 raise ValueError(f"request {req.rid} needs {need/1e9:.1f} GB, more than the cap")
             if self.used + need > self.cap:
@@ -185,7 +192,7 @@ class Server:
             queue.pop(0)
             p, flag = fut.result()
             del prepared[req.rid]
-            s = make_solver(req, p, flag, self.device)
+            s = make_solver(req, p, flag, self.device, self.pattern)
             if req.dtype not in self._tuned:             # the storage type's step configurations, once
                 s.autotune()
                 self._tuned.add(req.dtype)
@@ -358,10 +365,10 @@ class PlainServer:
         return reqs
 
 
-def run_alone(req, device="cuda", mode="graph"):
+def run_alone(req, device="cuda", mode="graph", pattern="ab"):
     """The same request solved by itself (its own batch), for alone-vs-mix checks and FP64 references."""
     p, flag = prepare(req)
-    s = make_solver(req, p, flag, device)
+    s = make_solver(req, p, flag, device, pattern)
     b = Batch(dtype=req.dtype, chunk=50, max_members=4, device=device, mode=mode)
     b.add(s)
     b.run()
@@ -386,6 +393,8 @@ def main(argv=None):
     ap.add_argument("--no-drain", action="store_true", help="stop at the end of the window (unfinished solves count as not done)")
     ap.add_argument("--fp64-check", type=int, default=0, help="re-run this many completed requests in float64")
     ap.add_argument("--host-masks", action="store_true", help="pack the stone masks on the host instead of the GPU")
+    ap.add_argument("--pattern", default="ab", choices=["ab", "aa"],
+                    help="aa: solve every request in place (one lattice, graph mode)")
     a = ap.parse_args(argv)
     reqs = poisson_requests(a.rate, a.minutes * 60.0, seed=a.seed, H_range=(a.h_lo, a.h_hi),
                             steps=(a.steps_lo, a.steps_hi), f16_share=a.f16_share)
@@ -393,12 +402,12 @@ def main(argv=None):
         srv = PlainServer(chunk=a.chunk, mask_device=None if a.host_masks else "cuda")
     else:
         srv = Server(cap_bytes=a.cap_gb * 1e9, chunk=a.chunk, mode=a.mode, max_cells=a.max_cells or None,
-                     mask_device=None if a.host_masks else "cuda")
+                     mask_device=None if a.host_masks else "cuda", pattern=a.pattern)
     t0 = time.monotonic()
     out = srv.serve(reqs, max_seconds=a.minutes * 60.0, drain=not a.no_drain)
     elapsed = time.monotonic() - t0
     summ = Server.summary(out, elapsed)
-    summ.update(form="plain (float32, one at a time)" if a.plain else f"batched ({a.mode})",
+    summ.update(form="plain (float32, one at a time)" if a.plain else f"batched ({a.mode}, pattern {a.pattern})",
                 unfinished_at_end=srv.unfinished,
                 max_resident_gb=round(srv.max_used / 1e9, 2), cap_gb=a.cap_gb, arrivals_per_s=a.rate,
                 window_minutes=a.minutes, seed=a.seed, drained=not a.no_drain)

@@ -209,8 +209,8 @@ def test_server_fails_only_the_diverged_request(monkeypatch, cuda):
             for i, dt in enumerate(["f16", "f16", "f32", "f16"])]
     orig = serve.make_solver
 
-    def planted(req, p, flag, device="cuda"):
-        s = orig(req, p, flag, device)
+    def planted(req, p, flag, device="cuda", pattern="ab"):
+        s = orig(req, p, flag, device, pattern)
         if req.rid == 1:
             s.state.assign(_poison(s.state.numpy(), flag))
         return s

@@ -43,6 +43,23 @@ def test_result_is_the_same_alone_and_in_the_mix(mode, cuda):
             assert v == r.result["stats"][k] or (np.isnan(v) and np.isnan(r.result["stats"][k])), (r.rid, k)
 
 
+def test_server_solves_in_place(cuda):
+    """pattern "aa": every request on one lattice (smaller footprint), odd chunks carry the AA
+    parity; each result equals the same request solved alone in place."""
+    from stonewall.serve import Server, footprint, run_alone, solve_stats
+    reqs = _requests()
+    assert all(footprint(r, "aa") < footprint(r) for r in reqs)
+    srv = Server(cap_bytes=1e12, chunk=15, pattern="aa")
+    out = srv.serve(reqs)
+    assert all(r.result is not None and "failed" not in r.result for r in out)
+    for r in out[:3]:
+        st = solve_stats(run_alone(r, pattern="aa"))
+        for k, v in st.items():
+            assert v == r.result["stats"][k] or (np.isnan(v) and np.isnan(r.result["stats"][k])), (r.rid, k)
+    with pytest.raises(ValueError):
+        Server(pattern="aa", mode="persistent")
+
+
 def test_plain_form_serves_the_same_stream(cuda):
     """The comparison form: one float32 solve at a time, first come first served."""
     from stonewall.serve import PlainServer, Server

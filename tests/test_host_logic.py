@@ -92,7 +92,7 @@ def test_server_admission_rules(monkeypatch):
         def add(self, s):
             self.members.append(s)
 
-    def fake_solver(req, p, flag, device):
+    def fake_solver(req, p, flag, device, pattern="ab"):
         return SimpleNamespace(grid=SimpleNamespace(cells=S.cells_of(req)), autotune=lambda: None, t=0,
                                n_total=req.steps)
 
@@ -102,7 +102,7 @@ def test_server_admission_rules(monkeypatch):
     done.set_result((None, None))
     srv = object.__new__(S.Server)
     srv.cap, srv.max_cells, srv.cells, srv.used, srv.device = 3.2 * max(S.footprint(r) for r in reqs), float("inf"), 0, 0.0, None
-    srv.resident, srv._tuned = {}, set()
+    srv.resident, srv._tuned, srv.pattern = {}, set(), "ab"
     srv.batches = {"f32": FakeBatch(2), "f16": FakeBatch(2)}
     queue = list(reqs)
     srv._admit(queue, {r.rid: done for r in reqs}, 0.0)
