@@ -293,7 +293,14 @@ class Batch:
         Returns (best, times): best is a configuration number or "graph"."""
         times = {}
         if any(getattr(m, "pattern", "ab") == "aa" for m in self.members):
-            return "graph", times                    # in-place members: graph mode, and no trial steps
+            # in-place members: graph mode, and no trial steps (they would change those states); the
+            # two-lattice members' configurations are still tuned on the largest of them
+            ab = [m for m in self.pending() if getattr(m, "pattern", "ab") == "ab"]
+            if ab:
+                from . import autotune as single
+                single.tune(max(ab, key=lambda m: m.grid.cells))
+            self.mode = "graph"
+            return "graph", times
         if "persistent" in modes:
             for cfg in range(N.lib().sw_step_config_count()):
                 if not _valid(self.dtype, cfg):

@@ -130,14 +130,14 @@ def test_aa_members_in_graph_mode_equal_their_solo_runs(dtype, cuda):
     across chunks): every member ends with the bits of its own solo run."""
     from stonewall.batch import Batch
     plan = [(SHAPES[0], "aa", 40), (SHAPES[1], "ab", 40), (SHAPES[2], "aa", 26)]
+    b = Batch(dtype=dtype, chunk=7, mode="graph")
+    ms = [b.add(_member(shape, seed, n, 9, dtype, pattern)) for (shape, seed), pattern, n in plan]
+    assert b.autotune()[0] == "graph"              # installs the two-lattice member's configuration
     solo = []
     for (shape, seed), pattern, n in plan:
         r = _member(shape, seed, n, 9, dtype, pattern)
         r.advance(n, use_graphs=False)
         solo.append(_snapshot(r))
-    b = Batch(dtype=dtype, chunk=7, mode="graph")
-    ms = [b.add(_member(shape, seed, n, 9, dtype, pattern)) for (shape, seed), pattern, n in plan]
-    assert b.autotune()[0] == "graph"
     b.advance(40)
     assert not b.pending()
     for want, m in zip(solo, ms):
